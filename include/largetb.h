@@ -1,0 +1,230 @@
+/*
+ * largetb.h -- C-ABI of the GB300 (sm_103a) density-matrix hot path for the
+ * largeTB self-consistent-charge tight-binding code.
+ *
+ * The reference (pghale/largeTB, withSP2_deltaH.cpp / withSP2.cpp) runs this
+ * path as PETSc CPU code on file-scope globals: runKPM() and
+ * computeDensityMatrix() read the assembled AIJ matrix Htotal, the
+ * orbital2Atom map and Nelectrons, and write muval, diagP and chargeOnAtom;
+ * constructdeltaH()/updateHtotal() close the SCC loop.  This header replaces
+ * those entry points with explicit, re-entrant calls on a context that owns
+ * one CUDA device stream.  Conventions:
+ *
+ *   - Every function returns an int status: TB_OK (0) or a positive error
+ *     code, like PetscErrorCode.  No C++ exception crosses this boundary.
+ *     tb_last_error() gives the message of the last failure on a context.
+ *   - Inputs are plain host arrays, copied during the call; the caller keeps
+ *     ownership.  Outputs are caller-owned host arrays.  Every call is
+ *     synchronous at return (like the reference's collective PETSc calls).
+ *   - One context per host thread; a context is not thread-safe.
+ *   - Units: bohr, Hartree, electrons.  Orbitals are 4 per atom (s, px, py,
+ *     pz), contiguous: orbital i belongs to atom i/4, as the reference's
+ *     localBeginIndex/localEndIndex layout (withSP2_deltaH.cpp:525-664).
+ *   - Charges are electron counts over both spins: q_a = 2 sum_{i in a} P_ii;
+ *     diagP is per spin (the reference's diagP, withSP2_deltaH.cpp:1375).
+ *   - There is no CPU fallback: without a usable CUDA device every compute
+ *     call returns TB_ERR_NO_DEVICE.
+ */
+#ifndef LARGETB_H
+#define LARGETB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TB_ABI_VERSION 1
+
+enum tb_status {
+    TB_OK = 0,
+    TB_ERR_INVALID_ARG = 1,   /* null pointer, bad size, bad parameter */
+    TB_ERR_STRUCTURE = 2,     /* CSR not sorted/in range, or orb2atom not 4-per-atom contiguous */
+    TB_ERR_NONFINITE = 3,     /* NaN or Inf in an input */
+    TB_ERR_NOT_READY = 4,     /* Hamiltonian or SCC data not set */
+    TB_ERR_SPECTRUM = 5,      /* Gershgorin interval collapsed (lmax <= lmin) */
+    TB_ERR_BISECTION = 6,     /* electron count not bracketed by mu in [lmin, lmax] */
+    TB_ERR_NOT_CONVERGED = 7, /* SCC or SP2 stopped at its iteration cap */
+    TB_ERR_DIVERGED = 8,      /* SCC charges left any physical range */
+    TB_ERR_CUDA = 9,          /* CUDA runtime error; message in tb_last_error */
+    TB_ERR_NO_DEVICE = 10,    /* no CUDA device of compute capability 10.3 */
+    TB_ERR_OUT_OF_MEMORY = 11,
+    TB_ERR_UNSUPPORTED = 12
+};
+
+enum tb_precision {
+    TB_PREC_FP64 = 0, /* plain form: FP64 recurrence, T_{k+1} = 2 X T_k - T_{k-1} */
+    TB_PREC_FP32 = 1  /* FP32 recurrence to order M/2 with FP64-accumulated moments
+                         from T_{2k} = 2 T_k^2 - 1, T_{2k+1} = 2 T_k T_{k+1} - X */
+};
+
+enum tb_kernel_kind {
+    TB_KERNEL_JACKSON = 0,  /* closed form of runKPM, withSP2_deltaH.cpp:1593-1595 */
+    TB_KERNEL_AUTOCORR = 1, /* getKPE's autocorrelation form, withSP2_deltaH.cpp:1104-1132 */
+    TB_KERNEL_NONE = 2
+};
+
+typedef struct tb_params {
+    uint32_t struct_size;  /* sizeof(tb_params); set by tb_params_init */
+    int32_t M;             /* expansion terms n = 0..M-1 (getKPE's M, withSP2_deltaH.cpp:1094);
+                              2 <= M <= 6000 */
+    int32_t kernel;        /* enum tb_kernel_kind */
+    int32_t precision;     /* enum tb_precision */
+    double kT;             /* electronic temperature, Hartree; <= 0 selects the step
+                              function of getKPE (withSP2_deltaH.cpp:1100-1103) */
+    double n_electrons;    /* electrons, both spins; <= 0 takes sum(q0) from tb_set_scc */
+    int32_t column_block;  /* identity columns per slab; 0 = autotune */
+    int32_t device;        /* CUDA device ordinal */
+    double spectral_pad;   /* relative widening of the Gershgorin interval */
+    double mu_tol;         /* bisection tolerance on the electron count */
+    double scc_tol;        /* convergence: max_a |q_out - q_in| < scc_tol (electrons) */
+    int32_t scc_max_iter;
+    int32_t mix_history;   /* Anderson mixing depth, 0 = linear mixing (max 16) */
+    double mix_beta;       /* mixing parameter */
+    double sp2_drop_tol;   /* SP2: drop 4x4 blocks with Frobenius norm below this */
+    int32_t sp2_max_iter;
+    int32_t reserved0;
+    double sp2_idem_tol;   /* SP2: stop when ||X^2 - X||_F < sp2_idem_tol */
+    double reserved[6];
+} tb_params;
+
+typedef struct tb_report {
+    double lmin, lmax;        /* Gershgorin bounds of the last density evaluation */
+    double a, b;              /* X = (H - b)/a */
+    double mu;                /* chemical potential, Hartree */
+    double n_electrons_found; /* 2 sum_n c_n g_n mu_n at the returned mu */
+    double e_band;            /* 2 tr(P H) */
+    double dq_max;            /* last SCC residual max_a |q_out - q_in| */
+    int32_t scc_iters;        /* density evaluations performed */
+    int32_t bisect_rounds;
+    int32_t column_block;     /* slab width used */
+    int32_t precision;
+    double t_total_ms;        /* CUDA-event time of the call on the context stream */
+    double t_moments_ms;      /* CUDA-event time of the Chebyshev moment passes */
+    int64_t spmm_launches;    /* Chebyshev step kernel launches */
+    double spmm_bytes;        /* algorithmic bytes moved by those launches */
+    int64_t kernel_launches;  /* all kernels this call launched */
+    double asym_max;          /* max |H_ij - H_ji| seen by tb_set_hamiltonian */
+    double idem_err;          /* SP2: ||X^2 - X||_F of the returned X */
+    int32_t sp2_iters;
+    int32_t reserved0;
+    int64_t sp2_nnzb;         /* SP2: stored blocks of the returned X */
+    double reserved[8];
+} tb_report;
+
+typedef struct tb_ctx tb_ctx;
+
+/* Fill *p with defaults (M = 200, Jackson, kT = 0.01, FP64, Anderson 8 / 0.2,
+ * scc_tol = 1e-6, SP2 drop 1e-5 / 40 iterations). */
+int tb_params_init(tb_params *p);
+
+/* Create a context on p->device.  Replaces PetscInitialize + the global state
+ * of withSP2_deltaH.cpp:26-66.  Returns TB_ERR_NO_DEVICE without an sm_103
+ * device. */
+int tb_ctx_create(const tb_params *p, tb_ctx **out);
+int tb_ctx_destroy(tb_ctx *ctx);
+
+/* Replace the parameters of an existing context (precision, M, kT, ...). */
+int tb_set_params(tb_ctx *ctx, const tb_params *p);
+int tb_get_params(const tb_ctx *ctx, tb_params *p);
+
+/* The assembled Hamiltonian Htotal as PETSc seqaij i/j/a arrays (what
+ * MatGetRowIJ + MatSeqAIJGetArrayRead return) plus the orbital -> atom map
+ * (row i of orbital2Atom, withSP2_deltaH.cpp:905-922).  Replaces the
+ * MatSetValues(H/Htotal) assembly of constructH (withSP2_deltaH.cpp:969-1066)
+ * as the input of runKPM.  n = 4 * natoms; column indices within a row must
+ * be strictly increasing.  Missing transposed entries are filled and the
+ * matrix is symmetrised as (H + H^T)/2 (runKPM, withSP2_deltaH.cpp:1536-1538);
+ * the largest asymmetry is reported in tb_report.asym_max. */
+int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int32_t *colidx,
+                       const double *vals, const int32_t *orb2atom, int32_t natoms);
+
+/* Gamma_ab as CSR (natoms x natoms) and the neutral electron counts q0 of
+ * each atom.  Replaces initializeForSCF (withSP2_deltaH.cpp:854-967) and the
+ * neutralCharges vector (withSP2_deltaH.cpp:713-720). */
+int tb_set_scc(tb_ctx *ctx, int32_t natoms, const int32_t *g_rowptr, const int32_t *g_colidx,
+               const double *g_vals, const double *q0);
+
+/* Gershgorin bounds of H + diag(shift) (shift may be NULL).
+ * Replaces GershGorinParallel, withSP2_deltaH.cpp:144-209. */
+int tb_gershgorin(tb_ctx *ctx, const double *shift, double *lmin, double *lmax);
+
+/* One density evaluation of H + diag(shift) (shift: n values or NULL):
+ * Gershgorin scaling, exact-trace Chebyshev moments over identity column
+ * slabs, Jackson damping, mu bisection on the electron count, then diagP (n),
+ * q (natoms), e_band, mu and the moments mu_k = tr T_k(X), k = 0..M
+ * (moments may be NULL).  Replaces runKPM + computeDensityMatrix
+ * (withSP2_deltaH.cpp:1401-1411, 1528-1723) with the exact trace the
+ * reference leaves commented out (lines 1361-1379). */
+int tb_density(tb_ctx *ctx, const double *shift, double *diagP, double *q, double *e_band,
+               double *mu, double *moments, tb_report *rep);
+
+/* Coulomb shift V = Gamma (q - q0) per atom (natoms).  Replaces the
+ * netCharges/gammaq steps of constructdeltaH, withSP2_deltaH.cpp:1424-1429;
+ * the orbital shift of atom a is V_a on its four diagonal entries
+ * (withSP2_deltaH.cpp:1443-1459). */
+int tb_coulomb_shift(tb_ctx *ctx, const double *q, double *V);
+
+/* Self-consistent charges: H = H0 + diag(V(q_in)), density, Anderson mixing,
+ * until max_a |q_out - q_in| < scc_tol.  q_init may be NULL (start from q0).
+ * Replaces the SCC loop of main, withSP2_deltaH.cpp:1820-1840 (which never
+ * adds delta H: mixRatio = 0 at line 56).  Outputs: q and diagP of the last
+ * evaluation, e_band, mu, iteration count.  Returns TB_ERR_NOT_CONVERGED at
+ * scc_max_iter (outputs still written). */
+int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, double *e_band,
+                 double *mu, int32_t *iters, tb_report *rep);
+
+/* SP2 purification of H as a thresholded 4x4 block SpGEMM (FP32 blocks with
+ * FP64 traces when precision is TB_PREC_FP32, FP64 otherwise).  X0 from the
+ * Gershgorin bounds; per step X <- X^2 if 2 tr X > N_e else 2X - X^2
+ * (computeAlphas branch rule, withSP2.cpp:1027-1030; getSP2 recursion,
+ * withSP2.cpp:956-984).  Outputs diagP, q, e_band = 2 tr(X H); the report
+ * carries iterations, ||X^2 - X||_F and the stored block count. */
+int tb_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep);
+
+/* Stochastic KPM density of states of H (runKPM's DOS, withSP2_deltaH.cpp:1579-1648):
+ * n_random Gaussian vectors (counter-based splitmix64/Box-Muller with `seed`),
+ * n_moments Jackson-damped moments, the DOS at npts Chebyshev nodes.  Writes
+ * moments (n_moments), energies and dos (npts each). */
+int tb_kpm_dos(tb_ctx *ctx, int32_t n_moments, int32_t n_random, uint64_t seed, int32_t npts,
+               double *moments, double *energies, double *dos, tb_report *rep);
+
+/* Message of the last failure on ctx (never NULL). */
+const char *tb_last_error(const tb_ctx *ctx);
+const char *tb_status_string(int status);
+int tb_abi_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Model builder: upstream of the boundary.  Builds what the reference's     */
+/* arrangeCoordinates/constructH/initializeForSCF produce, for synthetic     */
+/* inputs: the reference's alpha-quartz cell, or beta-cristobalite.          */
+/* ------------------------------------------------------------------------ */
+typedef struct tb_model tb_model;
+
+/* alpha-quartz L x M x N exactly as the reference builds it (x/y periodic,
+ * 0.1 < d^2 < 16 bohr^2, Gamma diagonal -1): withSP2_deltaH.cpp:372-740, 854-1066. */
+int tb_model_quartz(int32_t L, int32_t M, int32_t N, tb_model **out);
+
+/* beta-cristobalite nx x ny x nz conventional cells (24 atoms each), edge
+ * a_ang, Gaussian displacements sigma_ang per Cartesian component from a
+ * counter-based splitmix64/Box-Muller stream with `seed`, 3-D periodic,
+ * neighbours within rcut_bohr, reference block model, Gamma diagonal
+ * gamma_diag (+1: Hubbard U = 1 Ha with the physical sign). */
+int tb_model_cristobalite(int32_t nx, int32_t ny, int32_t nz, double a_ang, double sigma_ang,
+                          uint64_t seed, double rcut_bohr, double gamma_diag, tb_model **out);
+
+int tb_model_sizes(const tb_model *m, int32_t *natoms, int32_t *n, int64_t *nnz,
+                   int64_t *g_nnz);
+
+/* Copy the model out (any pointer may be NULL): H CSR (n+1, nnz, nnz),
+ * orb2atom (n), Gamma CSR (natoms+1, g_nnz, g_nnz), q0 (natoms),
+ * xyz (3*natoms, bohr), species (natoms, atomic numbers). */
+int tb_model_export(const tb_model *m, int32_t *rowptr, int32_t *colidx, double *vals,
+                    int32_t *orb2atom, int32_t *g_rowptr, int32_t *g_colidx, double *g_vals,
+                    double *q0, double *xyz, int32_t *species);
+int tb_model_destroy(tb_model *m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,827 @@
+// tb_api.cpp -- host side of the C-ABI in include/largetb.h: context,
+// validation and CSR -> BSR conversion of the caller's PETSc-style AIJ
+// arrays, and the orchestration of one density evaluation / SCC solve on the
+// context stream.  No compute happens on the host: every numeric stage is a
+// kernel in tb_kpe.cu / tb_sp2.cu, and there is no CPU fallback.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tb_internal.h"
+
+using namespace tb;
+
+namespace {
+
+constexpr double kPi = 3.141592653589793238463;
+
+int fail(tb_ctx *ctx, int code, const std::string &msg)
+{
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+#define TB_CUDA(call)                                                                   \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? TB_ERR_OUT_OF_MEMORY     \
+                                                             : TB_ERR_CUDA,             \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));            \
+        }                                                                               \
+    } while (0)
+
+#define TB_TRY(expr)            \
+    do {                        \
+        int rc_ = (expr);       \
+        if (rc_ != TB_OK) return rc_; \
+    } while (0)
+
+template <typename T>
+void dfree(T *&p)
+{
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+template <typename T>
+int dalloc(tb_ctx *ctx, T *&p, size_t count)
+{
+    dfree(p);
+    if (count == 0) count = 1;
+    TB_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
+    return TB_OK;
+}
+
+template <typename T>
+int upload(tb_ctx *ctx, T *&p, const T *src, size_t count)
+{
+    TB_TRY(dalloc(ctx, p, count));
+    if (count) TB_CUDA(cudaMemcpyAsync(p, src, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return TB_OK;
+}
+
+int quad_nodes(int M, double beta_x)
+{
+    double need = 4.0 * M;
+    if (beta_x > 0 && 13.0 * beta_x > need) need = 13.0 * beta_x;
+    if (need < 256) need = 256;
+    int nq = 256;
+    while (nq < need && nq < (1 << 22)) nq *= 2;
+    return nq;
+}
+
+void damping(int kind, int M, std::vector<double> &g)
+{
+    g.assign(M, 1.0);
+    if (kind == TB_KERNEL_JACKSON) {
+        // closed form of runKPM (withSP2_deltaH.cpp:1593-1595) with N = M terms
+        const double N = M;
+        const double cotv = std::cos(kPi / (N + 1)) / std::sin(kPi / (N + 1));
+        for (int k = 0; k < M; k++)
+            g[k] = ((N - k + 1) * std::cos(kPi * k / (N + 1)) + std::sin(kPi * k / (N + 1)) * cotv) /
+                   (N + 1);
+    } else if (kind == TB_KERNEL_AUTOCORR) {
+        // getKPE's autocorrelation of normalised U_i(cos(pi/(M+2)))
+        // (withSP2_deltaH.cpp:1104-1132, including its i < M-m-1 bound)
+        std::vector<double> u(M);
+        const double al = std::acos(std::cos(kPi / (M + 2)));
+        double nrm = 0.0;
+        for (int m = 0; m < M; m++) {
+            u[m] = std::sin((m + 1) * al) / std::sin(al);
+            nrm += u[m] * u[m];
+        }
+        nrm = std::sqrt(nrm);
+        for (int m = 0; m < M; m++) u[m] /= nrm;
+        for (int m = 0; m < M; m++) {
+            double s = 0.0;
+            for (int i = 0; i < M - m - 1; i++) s += u[i] * u[m + i];
+            g[m] = s;
+        }
+    }
+    g[0] = 1.0;  // the n = 0 term carries no damping factor (getKPE, line 1136)
+}
+
+int check_params(tb_ctx *ctx, const tb_params *p)
+{
+    if (!p) return fail(ctx, TB_ERR_INVALID_ARG, "params is NULL");
+    if (p->struct_size != sizeof(tb_params))
+        return fail(ctx, TB_ERR_INVALID_ARG, "tb_params.struct_size mismatch (call tb_params_init)");
+    if (p->M < 2 || p->M > 6000) return fail(ctx, TB_ERR_INVALID_ARG, "M must be in [2, 6000]");
+    if (p->kernel < 0 || p->kernel > 2) return fail(ctx, TB_ERR_INVALID_ARG, "unknown kernel kind");
+    if (p->precision != TB_PREC_FP64 && p->precision != TB_PREC_FP32)
+        return fail(ctx, TB_ERR_INVALID_ARG, "unknown precision");
+    if (!std::isfinite(p->kT)) return fail(ctx, TB_ERR_INVALID_ARG, "kT not finite");
+    if (p->column_block < 0 || p->column_block % 128 != 0)
+        return fail(ctx, TB_ERR_INVALID_ARG, "column_block must be 0 or a multiple of 128");
+    if (!(p->spectral_pad >= 0) || !(p->mu_tol > 0) || !(p->scc_tol > 0) || p->scc_max_iter < 1)
+        return fail(ctx, TB_ERR_INVALID_ARG, "bad pad / tolerance / iteration cap");
+    if (p->mix_history < 0 || p->mix_history > kMaxHistory || !(p->mix_beta > 0))
+        return fail(ctx, TB_ERR_INVALID_ARG, "mix_history must be in [0,16], mix_beta > 0");
+    if (!(p->sp2_drop_tol >= 0) || p->sp2_max_iter < 1 || !(p->sp2_idem_tol >= 0))
+        return fail(ctx, TB_ERR_INVALID_ARG, "bad SP2 parameters");
+    return TB_OK;
+}
+
+int set_device(tb_ctx *ctx)
+{
+    TB_CUDA(cudaSetDevice(ctx->device));
+    return TB_OK;
+}
+
+// Work buffers sized for the current parameters and matrix.
+int ensure_work(tb_ctx *ctx)
+{
+    DevWork &w = ctx->w;
+    const DevMatrix &m = ctx->m;
+    const tb_params &p = ctx->p;
+    const int M = p.M;
+    int B = p.column_block;
+    if (B == 0) B = (p.precision == TB_PREC_FP32) ? 256 : 128;
+    {
+        const int nround = ((m.n + 127) / 128) * 128;
+        if (B > nround) B = nround;
+    }
+    const int K = (p.precision == TB_PREC_FP32) ? (M + 2) / 2 : 0;
+    const int rowgroups = (p.precision == TB_PREC_FP32) ? cheb_f32_rowgroups(m.nb) : 0;
+    // quadrature capacity from the Gershgorin width of H0 with a 2x margin
+    // for SCC shifts; the device flags TB_ERR_SPECTRUM if it is exceeded.
+    int nq_cap = 1 << 14;
+    if (p.kT > 0)
+        nq_cap = std::max(nq_cap, quad_nodes(M, 2.0 * (ctx->h0_lmax - ctx->h0_lmin) / p.kT));
+    const bool same = w.M == M && w.B == B && w.K == K && w.precision == p.precision &&
+                      w.rowgroups == rowgroups && w.nq_cap >= nq_cap && w.d && w.mom && w.T0 &&
+                      w.kernel == p.kernel;
+    if (same) return TB_OK;
+    w.kernel = p.kernel;
+    w.M = M;
+    w.B = B;
+    w.K = K;
+    w.rowgroups = rowgroups;
+    w.precision = p.precision;
+    w.nq_cap = nq_cap;
+    const size_t es = (p.precision == TB_PREC_FP32) ? 4 : 8;
+    w.slab_bytes = (size_t)m.n * B * es;
+    {
+        char *t0 = (char *)w.T0, *t1 = (char *)w.T1;
+        dfree(t0);
+        dfree(t1);
+        w.T0 = w.T1 = nullptr;
+        TB_TRY(dalloc(ctx, t0, w.slab_bytes));
+        TB_TRY(dalloc(ctx, t1, w.slab_bytes));
+        w.T0 = t0;
+        w.T1 = t1;
+    }
+    TB_TRY(dalloc(ctx, w.d, (size_t)(M + 1) * m.n));
+    TB_TRY(dalloc(ctx, w.mom, (size_t)M + 1));
+    TB_TRY(dalloc(ctx, w.c, (size_t)M));
+    TB_TRY(dalloc(ctx, w.rho, (size_t)w.nq_cap));
+    TB_TRY(dalloc(ctx, w.cand, (size_t)kBisectCand));
+    TB_TRY(dalloc(ctx, w.diagP, (size_t)m.n));
+    TB_TRY(dalloc(ctx, w.q, (size_t)m.natoms));
+    TB_TRY(dalloc(ctx, w.shift, (size_t)m.n));
+    if (!w.state) {
+        TB_TRY(dalloc(ctx, w.state, 1));
+        TB_CUDA(cudaMemsetAsync(w.state, 0, sizeof(DevState), ctx->stream));
+    }
+    if (p.precision == TB_PREC_FP32) {
+        w.partial_elems = (int64_t)K * rowgroups * B * 2;
+        TB_TRY(dalloc(ctx, w.partial, (size_t)w.partial_elems));
+    } else {
+        dfree(w.partial);
+        w.partial_elems = 0;
+    }
+    std::vector<double> g;
+    damping(p.kernel, M, g);
+    TB_TRY(upload(ctx, w.g, g.data(), g.size()));
+    if (p.precision == TB_PREC_FP32) {
+        if (!ctx->m.x32) TB_TRY(dalloc(ctx, ctx->m.x32, (size_t)m.nnzb * 16));
+    } else {
+        if (!ctx->m.x64) TB_TRY(dalloc(ctx, ctx->m.x64, (size_t)m.nnzb * 16));
+    }
+    return TB_OK;
+}
+
+// Algorithmic bytes of one Chebyshev step over one slab:
+// nnzb (16 s + 4) + (nb + 1) 4 + 3 n B s.
+double step_bytes(const DevMatrix &m, int B, int s)
+{
+    return (double)m.nnzb * (16.0 * s + 4.0) + (double)(m.nb + 1) * 4.0 + 3.0 * m.n * (double)B * s;
+}
+
+std::pair<cudaEvent_t, cudaEvent_t> next_events(tb_ctx *ctx)
+{
+    if (ctx->ev_used == ctx->moment_events.size()) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        ctx->moment_events.push_back({a, b});
+    }
+    return ctx->moment_events[ctx->ev_used++];
+}
+
+// One density evaluation of H0 + diag(w.shift); leaves diagP / q / state on
+// the device.  Kernels only; no host synchronisation.
+int density_eval(tb_ctx *ctx, bool have_shift)
+{
+    DevWork &w = ctx->w;
+    DevMatrix &m = ctx->m;
+    const tb_params &p = ctx->p;
+    cudaStream_t st = ctx->stream;
+    const int M = p.M, B = w.B;
+    const double *shift = have_shift ? w.shift : nullptr;
+    launch_gershgorin(st, m, shift, p.spectral_pad, p.kT, M, w.nq_cap, w.state);
+    launch_build_x(st, m, shift, p.precision, w.state);
+    ctx->launches += 2;
+
+    auto ev = next_events(ctx);
+    cudaEventRecord(ev.first, st);
+    const int nslab = (m.n + B - 1) / B;
+    for (int s = 0; s < nslab; s++) {
+        const int c0 = s * B;
+        launch_slab_identity(st, w.T0, m.n, B, c0, p.precision);
+        ctx->launches++;
+        if (p.precision == TB_PREC_FP64) {
+            double *A = (double *)w.T0, *Bf = (double *)w.T1;
+            for (int kout = 1; kout <= M; kout++) {
+                const bool odd = kout & 1;
+                launch_cheb_step_f64(st, m, odd ? A : Bf, odd ? Bf : A, B, c0, kout == 1, w.d, kout);
+                ctx->launches += (kout == 1) ? 2 : 1;
+            }
+            ctx->spmm_launches += M;
+            ctx->spmm_bytes += M * step_bytes(m, B, 8);
+        } else {
+            float *A = (float *)w.T0, *Bf = (float *)w.T1;
+            for (int k = 0; k < w.K; k++) {
+                const int kout = k + 1;
+                const bool odd = kout & 1;
+                launch_cheb_step_f32(st, m, odd ? A : Bf, odd ? Bf : A, B, k == 0,
+                                     w.partial + (int64_t)k * w.rowgroups * B * 2, w.rowgroups);
+                ctx->launches++;
+            }
+            launch_f32_finalize(st, m, w.partial, w.K, w.rowgroups, B, c0, w.d, M);
+            ctx->launches++;
+            ctx->spmm_launches += w.K;
+            ctx->spmm_bytes += w.K * step_bytes(m, B, 4);
+        }
+    }
+    cudaEventRecord(ev.second, st);
+
+    launch_moment_sums(st, w.d, m.n, M + 1, w.mom);
+    ctx->launches++;
+    if (p.kT > 0) {
+        launch_dos_nodes(st, w.g, w.mom, M, w.state, w.nq_cap, w.rho);
+        ctx->launches++;
+    }
+    for (int r = 0; r < kBisectRounds; r++) {
+        launch_bisect_round(st, w.rho, w.g, w.mom, M, ctx->p.n_electrons, p.mu_tol, r, w.cand,
+                            w.state);
+        ctx->launches++;
+    }
+    launch_fermi_coeffs(st, M, w.state, w.c);
+    launch_charges(st, w.d, w.c, w.g, w.mom, M, m.n, m.natoms, w.diagP, w.q, w.state);
+    ctx->launches += 3;
+    TB_CUDA(cudaGetLastError());
+    return TB_OK;
+}
+
+int read_state(tb_ctx *ctx, DevState &hs)
+{
+    TB_CUDA(cudaMemcpyAsync(&hs, ctx->w.state, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+    TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    return TB_OK;
+}
+
+int state_status(tb_ctx *ctx, const DevState &hs)
+{
+    if (hs.status == TB_ERR_SPECTRUM)
+        return fail(ctx, TB_ERR_SPECTRUM, "Gershgorin interval collapsed or too wide for the quadrature");
+    if (hs.status == TB_ERR_BISECTION)
+        return fail(ctx, TB_ERR_BISECTION, "electron count not bracketed by mu in the spectrum");
+    if (hs.status == TB_ERR_DIVERGED) return fail(ctx, TB_ERR_DIVERGED, "SCC charges diverged");
+    if (hs.status != 0) return fail(ctx, hs.status, "device reported an error");
+    return TB_OK;
+}
+
+void begin_call(tb_ctx *ctx, cudaEvent_t *e0)
+{
+    ctx->launches = 0;
+    ctx->spmm_launches = 0;
+    ctx->spmm_bytes = 0.0;
+    ctx->ev_used = 0;
+    cudaEventCreate(e0);
+    cudaEventRecord(*e0, ctx->stream);
+}
+
+void fill_report(tb_ctx *ctx, cudaEvent_t e0, const DevState &hs, int iters, tb_report *rep)
+{
+    cudaEvent_t e1;
+    cudaEventCreate(&e1);
+    cudaEventRecord(e1, ctx->stream);
+    cudaEventSynchronize(e1);
+    float tot = 0.f;
+    cudaEventElapsedTime(&tot, e0, e1);
+    double tm = 0.0;
+    for (size_t i = 0; i < ctx->ev_used; i++) {
+        float x = 0.f;
+        cudaEventElapsedTime(&x, ctx->moment_events[i].first, ctx->moment_events[i].second);
+        tm += x;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!rep) return;
+    std::memset(rep, 0, sizeof(*rep));
+    rep->lmin = hs.lmin;
+    rep->lmax = hs.lmax;
+    rep->a = hs.a;
+    rep->b = hs.b;
+    rep->mu = hs.mu;
+    rep->n_electrons_found = hs.n_found;
+    rep->e_band = hs.e_band;
+    rep->dq_max = hs.dq_max;
+    rep->scc_iters = iters;
+    rep->bisect_rounds = hs.bisect_rounds;
+    rep->column_block = ctx->w.B;
+    rep->precision = ctx->p.precision;
+    rep->t_total_ms = tot;
+    rep->t_moments_ms = tm;
+    rep->spmm_launches = ctx->spmm_launches;
+    rep->spmm_bytes = ctx->spmm_bytes;
+    rep->kernel_launches = ctx->launches;
+    rep->asym_max = ctx->asym_max;
+}
+
+void free_all(tb_ctx *ctx)
+{
+    DevMatrix &m = ctx->m;
+    dfree(m.rowptr);
+    dfree(m.colidx);
+    dfree(m.diagblk);
+    dfree(m.blkrow);
+    dfree(m.h0);
+    dfree(m.h0diag);
+    dfree(m.radius);
+    dfree(m.x32);
+    dfree(m.x64);
+    dfree(m.xdiag32);
+    DevScc &s = ctx->s;
+    dfree(s.rowptr);
+    dfree(s.colidx);
+    dfree(s.val);
+    dfree(s.q0);
+    dfree(s.qin);
+    dfree(s.qout);
+    dfree(s.V);
+    dfree(s.hist_q);
+    dfree(s.hist_r);
+    dfree(s.hist_meta);
+    DevWork &w = ctx->w;
+    dfree(w.shift);
+    dfree(w.d);
+    dfree(w.mom);
+    dfree(w.g);
+    dfree(w.c);
+    dfree(w.rho);
+    dfree(w.cand);
+    dfree(w.diagP);
+    dfree(w.q);
+    dfree(w.partial);
+    dfree(w.state);
+    {
+        char *t0 = (char *)w.T0, *t1 = (char *)w.T1;
+        dfree(t0);
+        dfree(t1);
+        w.T0 = w.T1 = nullptr;
+    }
+    w = DevWork{};
+    if (ctx->sp2_scratch) cudaFree(ctx->sp2_scratch);
+    ctx->sp2_scratch = nullptr;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+int tb_abi_version(void) { return TB_ABI_VERSION; }
+
+const char *tb_status_string(int s)
+{
+    switch (s) {
+    case TB_OK: return "ok";
+    case TB_ERR_INVALID_ARG: return "invalid argument";
+    case TB_ERR_STRUCTURE: return "bad matrix structure";
+    case TB_ERR_NONFINITE: return "non-finite input";
+    case TB_ERR_NOT_READY: return "input not set";
+    case TB_ERR_SPECTRUM: return "spectral bounds unusable";
+    case TB_ERR_BISECTION: return "chemical potential not bracketed";
+    case TB_ERR_NOT_CONVERGED: return "iteration cap reached";
+    case TB_ERR_DIVERGED: return "SCC diverged";
+    case TB_ERR_CUDA: return "CUDA error";
+    case TB_ERR_NO_DEVICE: return "no sm_103 CUDA device";
+    case TB_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case TB_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+int tb_params_init(tb_params *p)
+{
+    if (!p) return TB_ERR_INVALID_ARG;
+    std::memset(p, 0, sizeof(*p));
+    p->struct_size = sizeof(tb_params);
+    p->M = 200;
+    p->kernel = TB_KERNEL_JACKSON;
+    p->precision = TB_PREC_FP64;
+    p->kT = 0.01;
+    p->n_electrons = 0.0;
+    p->column_block = 0;
+    p->device = 0;
+    p->spectral_pad = 0.0;
+    p->mu_tol = 1e-9;
+    p->scc_tol = 1e-6;
+    p->scc_max_iter = 100;
+    p->mix_history = 8;
+    p->mix_beta = 0.2;
+    p->sp2_drop_tol = 1e-5;
+    p->sp2_max_iter = 40;
+    p->sp2_idem_tol = 1e-10;
+    return TB_OK;
+}
+
+int tb_ctx_create(const tb_params *p, tb_ctx **out)
+{
+    if (!out) return TB_ERR_INVALID_ARG;
+    *out = nullptr;
+    int rc = check_params(nullptr, p);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p->device || p->device < 0) {
+        cudaGetLastError();
+        return TB_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, p->device) != cudaSuccess) return TB_ERR_NO_DEVICE;
+    if (!(prop.major == 10 && prop.minor == 3)) return TB_ERR_NO_DEVICE;
+    tb_ctx *ctx = new (std::nothrow) tb_ctx();
+    if (!ctx) return TB_ERR_OUT_OF_MEMORY;
+    ctx->p = *p;
+    ctx->device = p->device;
+    if (cudaSetDevice(ctx->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return TB_ERR_CUDA;
+    }
+    *out = ctx;
+    return TB_OK;
+}
+
+int tb_ctx_destroy(tb_ctx *ctx)
+{
+    if (!ctx) return TB_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_all(ctx);
+    for (auto &e : ctx->moment_events) {
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return TB_OK;
+}
+
+int tb_set_params(tb_ctx *ctx, const tb_params *p)
+{
+    if (!ctx) return TB_ERR_INVALID_ARG;
+    TB_TRY(check_params(ctx, p));
+    if (p->device != ctx->device) return fail(ctx, TB_ERR_INVALID_ARG, "device cannot change");
+    const double ne = ctx->p.n_electrons;
+    ctx->p = *p;
+    if (!(p->n_electrons > 0) && ctx->have_scc) ctx->p.n_electrons = ne;
+    return TB_OK;
+}
+
+int tb_get_params(const tb_ctx *ctx, tb_params *p)
+{
+    if (!ctx || !p) return TB_ERR_INVALID_ARG;
+    *p = ctx->p;
+    return TB_OK;
+}
+
+const char *tb_last_error(const tb_ctx *ctx)
+{
+    if (!ctx) return "no context";
+    return ctx->err.c_str();
+}
+
+int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int32_t *colidx,
+                       const double *vals, const int32_t *orb2atom, int32_t natoms)
+{
+    if (!ctx) return TB_ERR_INVALID_ARG;
+    if (n <= 0 || natoms <= 0 || !rowptr || !colidx || !vals || !orb2atom)
+        return fail(ctx, TB_ERR_INVALID_ARG, "null array or non-positive size");
+    if ((int64_t)natoms * 4 != n)
+        return fail(ctx, TB_ERR_STRUCTURE, "n must be 4 * natoms (sp3: 4 orbitals per atom)");
+    for (int i = 0; i < n; i++)
+        if (orb2atom[i] != i / 4)
+            return fail(ctx, TB_ERR_STRUCTURE,
+                        "orb2atom must map orbitals 4a..4a+3 to atom a (contiguous sp3 blocks)");
+    if (rowptr[0] != 0) return fail(ctx, TB_ERR_STRUCTURE, "rowptr[0] != 0");
+    for (int i = 0; i < n; i++) {
+        if (rowptr[i + 1] < rowptr[i]) return fail(ctx, TB_ERR_STRUCTURE, "rowptr not monotone");
+        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+            if (colidx[k] < 0 || colidx[k] >= n)
+                return fail(ctx, TB_ERR_STRUCTURE, "column index out of range");
+            if (k > rowptr[i] && colidx[k] <= colidx[k - 1])
+                return fail(ctx, TB_ERR_STRUCTURE, "column indices not strictly increasing");
+            if (!std::isfinite(vals[k])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in Hamiltonian");
+        }
+    }
+    TB_TRY(set_device(ctx));
+    const int nb = natoms;
+    // block pattern of H + H^T, diagonal always present
+    std::vector<std::vector<int32_t>> pat(nb);
+    for (int I = 0; I < nb; I++) pat[I].push_back(I);
+    for (int i = 0; i < n; i++)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+            const int I = i / 4, J = colidx[k] / 4;
+            pat[I].push_back(J);
+            pat[J].push_back(I);
+        }
+    std::vector<int32_t> brow(nb + 1, 0);
+    for (int I = 0; I < nb; I++) {
+        auto &v = pat[I];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        brow[I + 1] = brow[I] + (int32_t)v.size();
+    }
+    const int64_t nnzb = brow[nb];
+    std::vector<int32_t> bcol(nnzb), blkrow(nnzb), diagblk(nb);
+    for (int I = 0; I < nb; I++)
+        for (size_t t = 0; t < pat[I].size(); t++) {
+            bcol[brow[I] + t] = pat[I][t];
+            blkrow[brow[I] + t] = I;
+            if (pat[I][t] == I) diagblk[I] = brow[I] + (int32_t)t;
+        }
+    pat.clear();
+    pat.shrink_to_fit();
+    auto find_blk = [&](int I, int J) -> int64_t {
+        const int32_t *b = bcol.data() + brow[I], *e = bcol.data() + brow[I + 1];
+        const int32_t *it = std::lower_bound(b, e, J);
+        return (int64_t)(it - bcol.data());
+    };
+    // (H + H^T)/2 as runKPM forms it (withSP2_deltaH.cpp:1536-1538)
+    std::vector<double> blk((size_t)nnzb * 16, 0.0);
+    double asym = 0.0;
+    for (int i = 0; i < n; i++)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+            const int j = colidx[k];
+            const double v = vals[k];
+            const int64_t t1 = find_blk(i / 4, j / 4), t2 = find_blk(j / 4, i / 4);
+            blk[t1 * 16 + (i % 4) * 4 + (j % 4)] += 0.5 * v;
+            blk[t2 * 16 + (j % 4) * 4 + (i % 4)] += 0.5 * v;
+            const int32_t *b = colidx + rowptr[j], *e = colidx + rowptr[j + 1];
+            const int32_t *it = std::lower_bound(b, e, i);
+            const double vt = (it != e && *it == i) ? vals[rowptr[j] + (it - b)] : 0.0;
+            asym = std::max(asym, std::fabs(v - vt));
+        }
+    std::vector<double> h0diag(n), radius(n);
+    for (int I = 0; I < nb; I++)
+        for (int r = 0; r < 4; r++) {
+            double rad = 0.0, dg = 0.0;
+            for (int t = brow[I]; t < brow[I + 1]; t++)
+                for (int c = 0; c < 4; c++) {
+                    const double v = blk[(size_t)t * 16 + r * 4 + c];
+                    if (bcol[t] == I && c == r)
+                        dg = v;
+                    else
+                        rad += std::fabs(v);
+                }
+            h0diag[4 * I + r] = dg;
+            radius[4 * I + r] = rad;
+        }
+    free_all(ctx);
+    ctx->have_h = ctx->have_scc = false;
+    DevMatrix &m = ctx->m;
+    m.n = n;
+    m.natoms = natoms;
+    m.nb = nb;
+    m.nnzb = nnzb;
+    TB_TRY(upload(ctx, m.rowptr, brow.data(), brow.size()));
+    TB_TRY(upload(ctx, m.colidx, bcol.data(), bcol.size()));
+    TB_TRY(upload(ctx, m.blkrow, blkrow.data(), blkrow.size()));
+    TB_TRY(upload(ctx, m.diagblk, diagblk.data(), diagblk.size()));
+    TB_TRY(upload(ctx, m.h0, blk.data(), blk.size()));
+    TB_TRY(upload(ctx, m.h0diag, h0diag.data(), h0diag.size()));
+    TB_TRY(upload(ctx, m.radius, radius.data(), radius.size()));
+    TB_TRY(dalloc(ctx, m.xdiag32, (size_t)n));
+    // quadrature capacity: host Gershgorin width of H0, 2x margin for shifts
+    double mn = 1e300, mx = -1e300;
+    for (int i = 0; i < n; i++) {
+        mn = std::min(mn, h0diag[i] - radius[i]);
+        mx = std::max(mx, h0diag[i] + radius[i]);
+    }
+    ctx->h0_lmin = mn;
+    ctx->h0_lmax = mx;
+    TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->asym_max = asym;
+    ctx->have_h = true;
+    return TB_OK;
+}
+
+int tb_set_scc(tb_ctx *ctx, int32_t natoms, const int32_t *g_rowptr, const int32_t *g_colidx,
+               const double *g_vals, const double *q0)
+{
+    if (!ctx) return TB_ERR_INVALID_ARG;
+    if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "tb_set_hamiltonian must come first");
+    if (natoms != ctx->m.natoms || !g_rowptr || !g_colidx || !g_vals || !q0)
+        return fail(ctx, TB_ERR_INVALID_ARG, "natoms mismatch or null array");
+    if (g_rowptr[0] != 0) return fail(ctx, TB_ERR_STRUCTURE, "Gamma rowptr[0] != 0");
+    for (int a = 0; a < natoms; a++) {
+        if (g_rowptr[a + 1] < g_rowptr[a]) return fail(ctx, TB_ERR_STRUCTURE, "Gamma rowptr not monotone");
+        for (int k = g_rowptr[a]; k < g_rowptr[a + 1]; k++) {
+            if (g_colidx[k] < 0 || g_colidx[k] >= natoms)
+                return fail(ctx, TB_ERR_STRUCTURE, "Gamma column out of range");
+            if (!std::isfinite(g_vals[k])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in Gamma");
+        }
+        if (!std::isfinite(q0[a])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in q0");
+    }
+    TB_TRY(set_device(ctx));
+    DevScc &s = ctx->s;
+    s.natoms = natoms;
+    s.nnz = g_rowptr[natoms];
+    TB_TRY(upload(ctx, s.rowptr, g_rowptr, (size_t)natoms + 1));
+    TB_TRY(upload(ctx, s.colidx, g_colidx, (size_t)s.nnz));
+    TB_TRY(upload(ctx, s.val, g_vals, (size_t)s.nnz));
+    TB_TRY(upload(ctx, s.q0, q0, (size_t)natoms));
+    TB_TRY(dalloc(ctx, s.qin, (size_t)natoms));
+    TB_TRY(dalloc(ctx, s.qout, (size_t)natoms));
+    TB_TRY(dalloc(ctx, s.V, (size_t)natoms));
+    TB_TRY(dalloc(ctx, s.hist_q, (size_t)kMaxHistory * natoms));
+    TB_TRY(dalloc(ctx, s.hist_r, (size_t)kMaxHistory * natoms));
+    TB_TRY(dalloc(ctx, s.hist_meta, 2));
+    double ne = 0.0;
+    for (int a = 0; a < natoms; a++) ne += q0[a];
+    if (!(ctx->p.n_electrons > 0)) ctx->p.n_electrons = ne;
+    TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->have_scc = true;
+    return TB_OK;
+}
+
+int tb_gershgorin(tb_ctx *ctx, const double *shift, double *lmin, double *lmax)
+{
+    if (!ctx || !lmin || !lmax) return TB_ERR_INVALID_ARG;
+    if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian not set");
+    TB_TRY(set_device(ctx));
+    TB_TRY(ensure_work(ctx));
+    if (shift) TB_CUDA(cudaMemcpyAsync(ctx->w.shift, shift, sizeof(double) * ctx->m.n,
+                                       cudaMemcpyHostToDevice, ctx->stream));
+    launch_gershgorin(ctx->stream, ctx->m, shift ? ctx->w.shift : nullptr, 0.0, ctx->p.kT, ctx->p.M,
+                      ctx->w.nq_cap, ctx->w.state);
+    TB_CUDA(cudaGetLastError());
+    DevState hs;
+    TB_TRY(read_state(ctx, hs));
+    *lmin = hs.lmin;
+    *lmax = hs.lmax;
+    return TB_OK;
+}
+
+int tb_density(tb_ctx *ctx, const double *shift, double *diagP, double *q, double *e_band,
+               double *mu, double *moments, tb_report *rep)
+{
+    if (!ctx) return TB_ERR_INVALID_ARG;
+    if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian not set");
+    if (!(ctx->p.n_electrons > 0))
+        return fail(ctx, TB_ERR_NOT_READY, "n_electrons unset (give it in tb_params or tb_set_scc)");
+    if (shift)
+        for (int i = 0; i < ctx->m.n; i++)
+            if (!std::isfinite(shift[i])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in shift");
+    TB_TRY(set_device(ctx));
+    TB_TRY(ensure_work(ctx));
+    cudaEvent_t e0;
+    begin_call(ctx, &e0);
+    if (shift)
+        TB_CUDA(cudaMemcpyAsync(ctx->w.shift, shift, sizeof(double) * ctx->m.n,
+                                cudaMemcpyHostToDevice, ctx->stream));
+    TB_TRY(density_eval(ctx, shift != nullptr));
+    DevState hs;
+    TB_TRY(read_state(ctx, hs));
+    int rc = state_status(ctx, hs);
+    const size_t n = ctx->m.n, na = ctx->m.natoms;
+    if (diagP) TB_CUDA(cudaMemcpyAsync(diagP, ctx->w.diagP, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (q) TB_CUDA(cudaMemcpyAsync(q, ctx->w.q, na * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (moments)
+        TB_CUDA(cudaMemcpyAsync(moments, ctx->w.mom, (ctx->p.M + 1) * 8, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+    TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (e_band) *e_band = hs.e_band;
+    if (mu) *mu = hs.mu;
+    fill_report(ctx, e0, hs, 1, rep);
+    return rc;
+}
+
+int tb_coulomb_shift(tb_ctx *ctx, const double *q, double *V)
+{
+    if (!ctx || !q || !V) return TB_ERR_INVALID_ARG;
+    if (!ctx->have_scc) return fail(ctx, TB_ERR_NOT_READY, "SCC data not set");
+    TB_TRY(set_device(ctx));
+    const size_t na = ctx->s.natoms;
+    TB_CUDA(cudaMemcpyAsync(ctx->s.qout, q, na * 8, cudaMemcpyHostToDevice, ctx->stream));
+    launch_coulomb_shift(ctx->stream, ctx->s, ctx->s.qout, ctx->s.V, nullptr);
+    TB_CUDA(cudaGetLastError());
+    TB_CUDA(cudaMemcpyAsync(V, ctx->s.V, na * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    return TB_OK;
+}
+
+int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, double *e_band,
+                 double *mu, int32_t *iters, tb_report *rep)
+{
+    if (!ctx) return TB_ERR_INVALID_ARG;
+    if (!ctx->have_h || !ctx->have_scc)
+        return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian and SCC data must be set");
+    const size_t n = ctx->m.n, na = ctx->m.natoms;
+    if (q_init)
+        for (size_t a = 0; a < na; a++)
+            if (!std::isfinite(q_init[a])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in q_init");
+    TB_TRY(set_device(ctx));
+    TB_TRY(ensure_work(ctx));
+    cudaEvent_t e0;
+    begin_call(ctx, &e0);
+    cudaStream_t st = ctx->stream;
+    DevScc &s = ctx->s;
+    DevWork &w = ctx->w;
+    if (q_init)
+        TB_CUDA(cudaMemcpyAsync(s.qin, q_init, na * 8, cudaMemcpyHostToDevice, st));
+    else
+        TB_CUDA(cudaMemcpyAsync(s.qin, s.q0, na * 8, cudaMemcpyDeviceToDevice, st));
+    TB_CUDA(cudaMemsetAsync(s.hist_meta, 0, 2 * sizeof(int32_t), st));
+    TB_CUDA(cudaMemsetAsync(w.state, 0, sizeof(DevState), st));
+    launch_coulomb_shift(st, s, s.qin, s.V, w.shift);
+    ctx->launches++;
+    DevState hs;
+    std::memset(&hs, 0, sizeof(hs));
+    int it = 0, rc = TB_ERR_NOT_CONVERGED;
+    for (it = 1; it <= ctx->p.scc_max_iter; it++) {
+        TB_TRY(density_eval(ctx, true));
+        launch_scc_update(st, s, w.q, ctx->p.mix_beta, ctx->p.mix_history, ctx->p.scc_tol, w.shift,
+                          w.state);
+        ctx->launches++;
+        TB_CUDA(cudaGetLastError());
+        TB_TRY(read_state(ctx, hs));
+        if (hs.status) {
+            rc = state_status(ctx, hs);
+            break;
+        }
+        if (hs.converged) {
+            rc = TB_OK;
+            break;
+        }
+    }
+    if (it > ctx->p.scc_max_iter) {
+        it = ctx->p.scc_max_iter;
+        fail(ctx, TB_ERR_NOT_CONVERGED, "SCC reached scc_max_iter");
+    }
+    if (q) TB_CUDA(cudaMemcpyAsync(q, w.q, na * 8, cudaMemcpyDeviceToHost, st));
+    if (diagP) TB_CUDA(cudaMemcpyAsync(diagP, w.diagP, n * 8, cudaMemcpyDeviceToHost, st));
+    TB_CUDA(cudaStreamSynchronize(st));
+    if (e_band) *e_band = hs.e_band;
+    if (mu) *mu = hs.mu;
+    if (iters) *iters = it;
+    fill_report(ctx, e0, hs, it, rep);
+    return rc;
+}
+
+int tb_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep)
+{
+    (void)diagP;
+    (void)q;
+    (void)e_band;
+    (void)rep;
+    return fail(ctx, TB_ERR_UNSUPPORTED, "SP2 not built yet");
+}
+
+int tb_kpm_dos(tb_ctx *ctx, int32_t n_moments, int32_t n_random, uint64_t seed, int32_t npts,
+               double *moments, double *energies, double *dos, tb_report *rep)
+{
+    (void)n_moments;
+    (void)n_random;
+    (void)seed;
+    (void)npts;
+    (void)moments;
+    (void)energies;
+    (void)dos;
+    (void)rep;
+    return fail(ctx, TB_ERR_UNSUPPORTED, "stochastic DOS not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,143 @@
+// tb_internal.h -- shared declarations of the largeTB GB300 hot path
+// (context layout, device scratch, kernel launchers).  Not part of the ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/largetb.h"
+
+namespace tb {
+
+// Scalars of one density evaluation, resident in device memory so that a
+// whole SCC iteration runs without a host round trip.
+struct DevState {
+    double lmin, lmax, a, b;  // Gershgorin bounds, X = (H - b)/a
+    double lo, hi;            // bisection bracket (scaled units)
+    double mu_x, mu;          // chemical potential, scaled and Hartree
+    double n_found, e_band;
+    double dq_max;
+    double beta_x;            // a / kT (0: step function)
+    int32_t nq;               // quadrature nodes
+    int32_t bisect_done;
+    int32_t bisect_rounds;
+    int32_t status;           // enum tb_status raised on the device
+    int32_t converged;
+    uint32_t ticket;          // last-block counter of the multisection round
+};
+
+// Candidates evaluated per multisection round.
+constexpr int kBisectCand = 128;
+constexpr int kBisectRounds = 8;
+constexpr int kMaxHistory = 16;
+
+// Device buffers owned by a context.  All sizes in elements.
+struct DevMatrix {
+    int32_t n = 0, natoms = 0, nb = 0;
+    int64_t nnzb = 0;
+    int32_t *rowptr = nullptr;   // nb+1
+    int32_t *colidx = nullptr;   // nnzb
+    int32_t *diagblk = nullptr;  // nb: index of block (I,I)
+    int32_t *blkrow = nullptr;   // nnzb: block row of each stored block
+    double *h0 = nullptr;        // nnzb*16, symmetrised H blocks (row-major 4x4)
+    double *h0diag = nullptr;    // n
+    double *radius = nullptr;    // n, Gershgorin radius sum_{j!=i} |H_ij|
+    float *x32 = nullptr;        // nnzb*16 scaled blocks (FP32 form)
+    double *x64 = nullptr;       // nnzb*16 scaled blocks (FP64 form)
+    float *xdiag32 = nullptr;    // n, diagonal of the FP32 X actually used
+};
+
+struct DevScc {
+    int32_t natoms = 0;
+    int64_t nnz = 0;
+    int32_t *rowptr = nullptr, *colidx = nullptr;
+    double *val = nullptr;
+    double *q0 = nullptr;
+    double *qin = nullptr, *qout = nullptr;
+    double *V = nullptr;
+    double *hist_q = nullptr, *hist_r = nullptr;  // kMaxHistory * natoms
+    int32_t *hist_meta = nullptr;                 // {count, head}
+};
+
+struct DevWork {
+    int32_t M = 0, nq_cap = 0, B = 0, K = 0, rowgroups = 0;
+    int32_t precision = -1;
+    int32_t kernel = -1;
+    double *shift = nullptr;   // n
+    double *d = nullptr;       // (M+1) * n diagonal moments [k][i]
+    double *mom = nullptr;     // M+1
+    double *g = nullptr;       // M damping factors
+    double *c = nullptr;       // M expansion coefficients
+    double *rho = nullptr;     // nq damped DOS at the quadrature nodes
+    double *cand = nullptr;    // kBisectCand electron counts
+    double *diagP = nullptr;   // n
+    double *q = nullptr;       // natoms
+    double *partial = nullptr; // FP32 form: K * rowgroups * B * 2 dot partials
+    void *T0 = nullptr, *T1 = nullptr;  // slab buffers, n x B
+    size_t slab_bytes = 0;
+    int64_t partial_elems = 0;
+    DevState *state = nullptr;
+};
+
+}  // namespace tb
+
+struct tb_ctx {
+    tb_params p{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool have_h = false, have_scc = false;
+    double asym_max = 0.0;
+    double h0_lmin = 0.0, h0_lmax = 0.0;  // Gershgorin bounds of the unshifted H
+    tb::DevMatrix m;
+    tb::DevScc s;
+    tb::DevWork w;
+    int64_t launches = 0;
+    int64_t spmm_launches = 0;
+    double spmm_bytes = 0.0;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> moment_events;
+    size_t ev_used = 0;
+    int autotuned_B[2] = {0, 0};
+    // SP2 device scratch (lazily sized)
+    void *sp2_scratch = nullptr;
+    size_t sp2_scratch_bytes = 0;
+};
+
+namespace tb {
+
+// ---- launchers implemented in tb_kpe.cu ----------------------------------
+void launch_coulomb_shift(cudaStream_t st, const DevScc &s, const double *q, double *V,
+                          double *shift);
+void launch_gershgorin(cudaStream_t st, const DevMatrix &m, const double *shift, double pad,
+                       double kT, int M, int nq_cap, DevState *state);
+void launch_build_x(cudaStream_t st, const DevMatrix &m, const double *shift, int precision,
+                    const DevState *state);
+void launch_slab_identity(cudaStream_t st, void *T0, int n, int B, int c0, int precision);
+// One plain FP64 Chebyshev step on a slab: first != 0: Tout = X Tin, else
+// Tout = 2 X Tin - Tout; the slab's diagonal entries go to d[kout].
+void launch_cheb_step_f64(cudaStream_t st, const DevMatrix &m, const double *Tin, double *Tout,
+                          int B, int c0, int first, double *d, int kout);
+// One FP32 step with the fused column dot products of T_k.
+void launch_cheb_step_f32(cudaStream_t st, const DevMatrix &m, const float *Tin, float *Tout,
+                          int B, int first, double *partial_k, int rowgroups);
+int cheb_f32_rowgroups(int nb);
+void launch_f32_finalize(cudaStream_t st, const DevMatrix &m, const double *partial, int K,
+                         int rowgroups, int B, int c0, double *d, int M);
+void launch_moment_sums(cudaStream_t st, const double *d, int n, int nmom, double *mom);
+void launch_dos_nodes(cudaStream_t st, const double *g, const double *mom, int M,
+                      const DevState *state, int nq_cap, double *rho);
+void launch_bisect_round(cudaStream_t st, const double *rho, const double *g, const double *mom,
+                         int M, double n_elec, double tol_n, int round, double *cand,
+                         DevState *state);
+void launch_fermi_coeffs(cudaStream_t st, int M, DevState *state, double *c);
+void launch_charges(cudaStream_t st, const double *d, const double *c, const double *g,
+                    const double *mom, int M, int n, int natoms, double *diagP, double *q,
+                    DevState *state);
+void launch_scc_update(cudaStream_t st, DevScc &s, const double *qout, double beta, int history,
+                       double tol, double *shift, DevState *state);
+
+}  // namespace tb

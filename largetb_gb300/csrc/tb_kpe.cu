@@ -1,0 +1,843 @@
+// tb_kpe.cu -- sm_103a kernels of the exact-trace KPE density-matrix path.
+//
+// Layout in HBM (n orbitals, nb = n/4 block rows, nnzb stored 4x4 blocks):
+//   BSR: rowptr[nb+1], colidx[nnzb], blocks [nnzb][4][4] row-major (FP64 H0,
+//   FP32 or FP64 scaled X).  Slab vectors T_k: [n][B] row-major, the B
+//   identity columns of one slab contiguous per row, so a warp reads a
+//   4-row x 128-column tile of T_k as 4 coalesced 512-byte rows (FP32:
+//   one float4 per lane per row; FP64: one double2 per lane per row over 64
+//   columns).  Diagonal moments d[k][i] = [T_k(X)]_ii, FP64, moment-major.
+//
+// Kernel map to the reference (withSP2_deltaH.cpp):
+//   k_gershgorin        GershGorinParallel 144-209 + the a/b of runKPM 1548-1560
+//   k_build_x           MatShift(-b)/MatScale(1/a) of runKPM 1559-1560, with the
+//                       SCC diagonal shift of constructdeltaH 1443-1459
+//   k_cheb_f64          getKPE recurrence 1134-1168 on identity column slabs with
+//                       the unit-vector diagonal extraction of 1361-1379
+//   k_cheb_f32          same recurrence in FP32 to order M/2; moments from
+//                       T_{2k} = 2 T_k^2 - I and T_{2k+1} = 2 T_k T_{k+1} - X
+//                       (FP64-accumulated column dot products)
+//   k_moment_sums ..    tr T_k, damped DOS, mu bisection: runKPM 1579-1712
+//   k_fermi_coeffs      getKPE coefficients 1100-1103 (Fermi instead of step)
+//   k_charges           computeDiagonalElements 1375-1385 (diagP, orbital2Atom)
+//   k_scc_update        constructdeltaH 1424-1429 + the SCC loop 1820-1840
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "tb_internal.h"
+
+namespace tb {
+
+namespace {
+
+constexpr double kPi = 3.141592653589793238463;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_min(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Sum over a block of up to 1024 threads; result valid in every thread.
+__device__ double block_sum(double v, double *sh)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+    if (w == 0) t = warp_sum(t);
+    if (threadIdx.x == 0) sh[0] = t;
+    __syncthreads();
+    double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ double fermi(double x, double mu_x, double beta_x)
+{
+    const double t = beta_x * (x - mu_x);
+    if (t > 0) {
+        const double e = exp(-t);
+        return e / (1.0 + e);
+    }
+    return 1.0 / (1.0 + exp(t));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Coulomb shift V = Gamma (q - q0), orbital shift = V of the owning atom.
+// ---------------------------------------------------------------------------
+__global__ void k_coulomb_shift(int natoms, const int32_t *__restrict__ rp,
+                                const int32_t *__restrict__ ci, const double *__restrict__ gv,
+                                const double *__restrict__ q, const double *__restrict__ q0,
+                                double *__restrict__ V, double *__restrict__ shift)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natoms) return;
+    double s = 0.0;
+    for (int k = rp[a]; k < rp[a + 1]; k++) {
+        const int b = ci[k];
+        s += gv[k] * (q[b] - q0[b]);
+    }
+    if (V) V[a] = s;
+    if (shift) {
+        shift[4 * a + 0] = s;
+        shift[4 * a + 1] = s;
+        shift[4 * a + 2] = s;
+        shift[4 * a + 3] = s;
+    }
+}
+
+void launch_coulomb_shift(cudaStream_t st, const DevScc &s, const double *q, double *V,
+                          double *shift)
+{
+    const int T = 256;
+    k_coulomb_shift<<<(s.natoms + T - 1) / T, T, 0, st>>>(s.natoms, s.rowptr, s.colidx, s.val, q,
+                                                         s.q0, V, shift);
+}
+
+// ---------------------------------------------------------------------------
+// Gershgorin bounds of H0 + diag(shift) and the scaling X = (H - b)/a.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_gershgorin(int n, const double *__restrict__ h0diag,
+                                                     const double *__restrict__ radius,
+                                                     const double *__restrict__ shift,
+                                                     double pad, double kT, int M, int nq_cap,
+                                                     DevState *st)
+{
+    __shared__ double smin[32], smax[32];
+    double mn = INFINITY, mx = -INFINITY;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double c = h0diag[i] + (shift ? shift[i] : 0.0);
+        mn = fmin(mn, c - radius[i]);
+        mx = fmax(mx, c + radius[i]);
+    }
+    mn = warp_min(mn);
+    mx = warp_max(mx);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        smin[w] = mn;
+        smax[w] = mx;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        mn = lane < nw ? smin[lane] : INFINITY;
+        mx = lane < nw ? smax[lane] : -INFINITY;
+        mn = warp_min(mn);
+        mx = warp_max(mx);
+        if (lane == 0) {
+            st->lmin = mn;
+            st->lmax = mx;
+            const double half = 0.5 * (mx - mn);
+            const double a = half * (1.0 + pad);
+            st->a = a;
+            st->b = 0.5 * (mx + mn);
+            st->status = (a > 0 && isfinite(a)) ? 0 : TB_ERR_SPECTRUM;
+            st->beta_x = kT > 0 ? a / kT : 0.0;
+            // quadrature size rule shared with the oracle: next power of two
+            // >= max(4M, 13 beta_x, 256)
+            double need = 4.0 * M;
+            if (st->beta_x > 0 && 13.0 * st->beta_x > need) need = 13.0 * st->beta_x;
+            if (need < 256) need = 256;
+            int nq = 256;
+            while (nq < need && nq < (1 << 22)) nq *= 2;
+            if (nq > nq_cap) st->status = TB_ERR_SPECTRUM;
+            st->nq = nq > nq_cap ? nq_cap : nq;
+            st->bisect_done = 0;
+            st->bisect_rounds = 0;
+            st->lo = -1.0;
+            st->hi = 1.0;
+            st->converged = 0;
+            st->ticket = 0u;
+        }
+    }
+}
+
+void launch_gershgorin(cudaStream_t st, const DevMatrix &m, const double *shift, double pad,
+                            double kT, int M, int nq_cap, DevState *state)
+{
+    k_gershgorin<<<1, 1024, 0, st>>>(m.n, m.h0diag, m.radius, shift, pad, kT, M, nq_cap, state);
+}
+
+// ---------------------------------------------------------------------------
+// X = (H0 + diag(shift) - b I) / a on the stored blocks.
+// ---------------------------------------------------------------------------
+__global__ void k_build_x(int64_t nnzb, const int32_t *__restrict__ blkrow,
+                          const int32_t *__restrict__ colidx, const double *__restrict__ h0,
+                          const double *__restrict__ shift, const DevState *__restrict__ st,
+                          float *__restrict__ x32, double *__restrict__ x64,
+                          float *__restrict__ xdiag32)
+{
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nnzb * 16) return;
+    const int64_t t = e >> 4;
+    const int rc = (int)(e & 15), r = rc >> 2, c = rc & 3;
+    const double a = st->a, b = st->b;
+    double v = h0[e];
+    const int I = blkrow[t];
+    const bool diag = (colidx[t] == I) && (r == c);
+    if (diag) v = v + (shift ? shift[4 * I + r] : 0.0) - b;
+    v = v / a;
+    if (x64) x64[e] = v;
+    if (x32) {
+        x32[e] = (float)v;
+        if (diag && xdiag32) xdiag32[4 * I + r] = (float)v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Identity slab T_0 = E[:, c0:c0+B] (and d[0][i] = 1 for the plain form).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_slab_identity(T *__restrict__ T0, int n, int B, int c0)
+{
+    const int64_t tot = (int64_t)n * B;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / B), j = (int)(e % B);
+        T0[e] = (i == c0 + j) ? T(1) : T(0);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Plain FP64 Chebyshev step.  Warp = one block row x 64 columns; lane = 2
+// columns (double2).  Tout = X Tin (first) or 2 X Tin - Tout (in place over
+// T_{k-1}).  The diagonal entry of each slab column is written to d[kout].
+// ---------------------------------------------------------------------------
+constexpr int kF64Warps = 4;
+
+__global__ void __launch_bounds__(32 * kF64Warps)
+    k_cheb_f64(int nb, int n, const int32_t *__restrict__ rowptr,
+               const int32_t *__restrict__ colidx, const double *__restrict__ x64,
+               const double *__restrict__ Tin, double *__restrict__ Tout, int B, int c0,
+               int first, double *__restrict__ d, int kout)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int I = blockIdx.x * kF64Warps + w;
+    if (I >= nb) return;
+    const int col = blockIdx.y * 64 + lane * 2;
+    double acc[4][2];
+#pragma unroll
+    for (int r = 0; r < 4; r++) acc[r][0] = acc[r][1] = 0.0;
+    const int t0 = rowptr[I], t1 = rowptr[I + 1];
+    for (int t = t0; t < t1; t++) {
+        const int J = __ldg(colidx + t);
+        const double2 *xb = reinterpret_cast<const double2 *>(x64 + (int64_t)t * 16);
+        double x[16];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const double2 v = __ldg(xb + q);
+            x[2 * q] = v.x;
+            x[2 * q + 1] = v.y;
+        }
+        double2 tv[4];
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+            tv[m] = __ldg(reinterpret_cast<const double2 *>(Tin + (int64_t)(4 * J + m) * B + col));
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+                acc[r][0] = fma(x[4 * r + m], tv[m].x, acc[r][0]);
+                acc[r][1] = fma(x[4 * r + m], tv[m].y, acc[r][1]);
+            }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        double2 *dst = reinterpret_cast<double2 *>(Tout + (int64_t)(4 * I + r) * B + col);
+        double2 o;
+        if (first) {
+            o.x = acc[r][0];
+            o.y = acc[r][1];
+        } else {
+            const double2 p = *dst;
+            o.x = 2.0 * acc[r][0] - p.x;
+            o.y = 2.0 * acc[r][1] - p.y;
+        }
+        *dst = o;
+        const int i = 4 * I + r;
+        const int j = i - c0 - col;  // column offset inside this lane's pair
+        if (j == 0) d[(int64_t)kout * n + i] = o.x;
+        if (j == 1) d[(int64_t)kout * n + i] = o.y;
+    }
+}
+
+void launch_slab_identity(cudaStream_t st, void *T0, int n, int B, int c0, int precision)
+{
+    const int T = 256;
+    int64_t tot = (int64_t)n * B;
+    int blocks = (int)((tot + T - 1) / T);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (precision == TB_PREC_FP64)
+        k_slab_identity<double><<<blocks, T, 0, st>>>((double *)T0, n, B, c0);
+    else
+        k_slab_identity<float><<<blocks, T, 0, st>>>((float *)T0, n, B, c0);
+}
+
+__global__ void k_diag_one(double *d, int n, int c0, int B)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < B && c0 + j < n) d[c0 + j] = 1.0;
+}
+
+void launch_cheb_step_f64(cudaStream_t st, const DevMatrix &m, const double *Tin, double *Tout,
+                          int B, int c0, int first, double *d, int kout)
+{
+    if (first) k_diag_one<<<(B + 127) / 128, 128, 0, st>>>(d, m.n, c0, B);
+    dim3 grid((m.nb + kF64Warps - 1) / kF64Warps, B / 64);
+    k_cheb_f64<<<grid, 32 * kF64Warps, 0, st>>>(m.nb, m.n, m.rowptr, m.colidx, m.x64, Tin, Tout,
+                                                B, c0, first, d, kout);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 Chebyshev step with fused column dot products.
+// CTA = 8 warps sharing one 128-column chunk; warp w handles kRowsPerWarp
+// consecutive block rows; lane = 4 columns (float4).  For every column j the
+// CTA accumulates  <T_k, T_k>  and  <T_k, T_{k+1}>  over its rows (FP32 per
+// block row, FP64 across block rows and warps) and writes one FP64 partial
+// pair per column to partial_k[rowgroup][B][2].
+// ---------------------------------------------------------------------------
+constexpr int kF32Warps = 8;
+constexpr int kRowsPerWarp = 2;
+
+__global__ void __launch_bounds__(32 * kF32Warps)
+    k_cheb_f32(int nb, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ colidx,
+               const float *__restrict__ x32, const float *__restrict__ Tin,
+               float *__restrict__ Tout, int B, int first, double *__restrict__ partial_k)
+{
+    __shared__ double red[kF32Warps][128][2];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int chunk = blockIdx.y;
+    const int col = chunk * 128 + lane * 4;
+    const int Ibase = (blockIdx.x * kF32Warps + w) * kRowsPerWarp;
+    double see[4] = {0, 0, 0, 0}, seo[4] = {0, 0, 0, 0};
+#pragma unroll 1
+    for (int rr = 0; rr < kRowsPerWarp; rr++) {
+        const int I = Ibase + rr;
+        if (I >= nb) break;
+        float acc[4][4];
+        float own[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[r][c] = 0.f, own[r][c] = 0.f;
+        const int t0 = rowptr[I], t1 = rowptr[I + 1];
+#pragma unroll 1
+        for (int t = t0; t < t1; t++) {
+            const int J = __ldg(colidx + t);
+            const float4 *xb = reinterpret_cast<const float4 *>(x32 + (int64_t)t * 16);
+            float4 xr[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) xr[q] = __ldg(xb + q);
+            float4 tv[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++)
+                tv[m] = __ldg(reinterpret_cast<const float4 *>(Tin + (int64_t)(4 * J + m) * B + col));
+            if (J == I) {
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    own[m][0] = tv[m].x;
+                    own[m][1] = tv[m].y;
+                    own[m][2] = tv[m].z;
+                    own[m][3] = tv[m].w;
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const float xm[4] = {xr[r].x, xr[r].y, xr[r].z, xr[r].w};
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    acc[r][0] = fmaf(xm[m], tv[m].x, acc[r][0]);
+                    acc[r][1] = fmaf(xm[m], tv[m].y, acc[r][1]);
+                    acc[r][2] = fmaf(xm[m], tv[m].z, acc[r][2]);
+                    acc[r][3] = fmaf(xm[m], tv[m].w, acc[r][3]);
+                }
+            }
+        }
+        float ee[4] = {0.f, 0.f, 0.f, 0.f}, eo[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            float4 *dst = reinterpret_cast<float4 *>(Tout + (int64_t)(4 * I + r) * B + col);
+            float4 o;
+            if (first) {
+                o = make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+            } else {
+                const float4 p = *dst;
+                o.x = 2.f * acc[r][0] - p.x;
+                o.y = 2.f * acc[r][1] - p.y;
+                o.z = 2.f * acc[r][2] - p.z;
+                o.w = 2.f * acc[r][3] - p.w;
+            }
+            *dst = o;
+            const float ov[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                ee[c] = fmaf(own[r][c], own[r][c], ee[c]);
+                eo[c] = fmaf(own[r][c], ov[c], eo[c]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            see[c] += (double)ee[c];
+            seo[c] += (double)eo[c];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        red[w][lane * 4 + c][0] = see[c];
+        red[w][lane * 4 + c][1] = seo[c];
+    }
+    __syncthreads();
+    {
+        const int j = threadIdx.x >> 1, which = threadIdx.x & 1;  // 256 threads = 128 cols x 2
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < kF32Warps; q++) s += red[q][j][which];
+        partial_k[((int64_t)blockIdx.x * B + chunk * 128 + j) * 2 + which] = s;
+    }
+}
+
+int cheb_f32_rowgroups(int nb)
+{
+    const int per = kF32Warps * kRowsPerWarp;
+    return (nb + per - 1) / per;
+}
+
+void launch_cheb_step_f32(cudaStream_t st, const DevMatrix &m, const float *Tin, float *Tout,
+                          int B, int first, double *partial_k, int rowgroups)
+{
+    dim3 grid(rowgroups, B / 128);
+    k_cheb_f32<<<grid, 32 * kF32Warps, 0, st>>>(m.nb, m.rowptr, m.colidx, m.x32, Tin, Tout, B,
+                                                first, partial_k);
+}
+
+// Sum the per-rowgroup partials of a slab and turn them into moments:
+// d[2k][j] = 2 <T_k,T_k>_j - 1,  d[2k+1][j] = 2 <T_k,T_{k+1}>_j - X_jj.
+__global__ void k_f32_finalize(const double *__restrict__ partial, int K, int rowgroups, int B,
+                               int c0, int n, const float *__restrict__ xdiag32,
+                               double *__restrict__ d, int M)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = blockIdx.y;
+    if (j >= B || k >= K) return;
+    const int i = c0 + j;
+    if (i >= n) return;
+    double se = 0.0, so = 0.0;
+    const double *p = partial + (int64_t)k * rowgroups * B * 2;
+    for (int g = 0; g < rowgroups; g++) {
+        se += p[((int64_t)g * B + j) * 2 + 0];
+        so += p[((int64_t)g * B + j) * 2 + 1];
+    }
+    if (2 * k <= M) d[(int64_t)(2 * k) * n + i] = 2.0 * se - 1.0;
+    if (2 * k + 1 <= M) d[(int64_t)(2 * k + 1) * n + i] = 2.0 * so - (double)xdiag32[i];
+}
+
+void launch_f32_finalize(cudaStream_t st, const DevMatrix &m, const double *partial, int K,
+                         int rowgroups, int B, int c0, double *d, int M)
+{
+    dim3 grid((B + 127) / 128, K);
+    k_f32_finalize<<<grid, 128, 0, st>>>(partial, K, rowgroups, B, c0, m.n, m.xdiag32, d, M);
+}
+
+// ---------------------------------------------------------------------------
+// mu_k = sum_i d[k][i]  (deterministic block tree).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_moment_sums(const double *__restrict__ d, int n,
+                                                     double *__restrict__ mom)
+{
+    __shared__ double sh[32];
+    const int k = blockIdx.x;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += d[(int64_t)k * n + i];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) mom[k] = s;
+}
+
+void launch_moment_sums(cudaStream_t st, const double *d, int n, int nmom, double *mom)
+{
+    k_moment_sums<<<nmom, 256, 0, st>>>(d, n, mom);
+}
+
+// rho_q = g_0 mu_0 + 2 sum_{k>=1} g_k mu_k cos(k theta_q): the damped DOS at
+// the Chebyshev-Gauss nodes (times pi sin theta), nq read from the state.
+__global__ void k_dos_nodes(const double *__restrict__ g, const double *__restrict__ mom, int M,
+                            const DevState *__restrict__ st, int nq_cap, double *__restrict__ rho)
+{
+    const int nq = st->nq;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq && q < nq_cap;
+         q += gridDim.x * blockDim.x) {
+        const double th = kPi * (q + 0.5) / nq;
+        double s = g[0] * mom[0];
+        for (int k = 1; k < M; k++) s += 2.0 * g[k] * mom[k] * cos(k * th);
+        rho[q] = s;
+    }
+}
+
+void launch_dos_nodes(cudaStream_t st, const double *g, const double *mom, int M,
+                            const DevState *state, int nq_cap, double *rho)
+{
+    const int T = 256;
+    int blocks = (nq_cap + T - 1) / T;
+    if (blocks > 1024) blocks = 1024;
+    k_dos_nodes<<<blocks, T, 0, st>>>(g, mom, M, state, nq_cap, rho);
+}
+
+// ---------------------------------------------------------------------------
+// Multisection for mu_x: each CTA evaluates the electron count at one of
+// kBisectCand equispaced points of [lo, hi]; the last CTA to finish narrows
+// the bracket (or records a solution / a bracketing failure).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_bisect_round(const double *__restrict__ rho, const double *__restrict__ g,
+                   const double *__restrict__ mom, int M, double n_elec, double tol_n, int round,
+                   int last_round, double *__restrict__ cand, DevState *st)
+{
+    __shared__ double sh[32];
+    __shared__ int s_last;
+    if (st->bisect_done) return;
+    const int P = gridDim.x, p = blockIdx.x;
+    const double lo = st->lo, hi = st->hi;
+    const double mu = lo + (hi - lo) * (double)p / (double)(P - 1);
+    const double beta_x = st->beta_x;
+    double s = 0.0;
+    if (beta_x > 0) {
+        const int nq = st->nq;
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            const double x = cos(kPi * (q + 0.5) / nq);
+            s += fermi(x, mu, beta_x) * rho[q];
+        }
+        s = block_sum(s, sh);
+        s = 2.0 * s / nq;
+    } else {
+        const double th = acos(mu);
+        for (int k = threadIdx.x; k < M; k += blockDim.x) {
+            const double c = (k == 0) ? 1.0 - th / kPi : -2.0 * sin(k * th) / (k * kPi);
+            s += c * g[k] * mom[k];
+        }
+        s = block_sum(s, sh);
+        s = 2.0 * s;
+    }
+    if (threadIdx.x == 0) {
+        cand[p] = s;
+        __threadfence();
+        const unsigned int t = atomicAdd(&st->ticket, 1u);
+        s_last = (t == (unsigned)(P - 1));
+    }
+    __syncthreads();
+    if (!s_last || threadIdx.x != 0) return;
+    __threadfence();
+    st->ticket = 0u;
+    volatile double *vc = cand;
+    st->bisect_rounds = round + 1;
+    if (round == 0 && !(vc[0] <= n_elec && n_elec <= vc[P - 1])) {
+        st->status = TB_ERR_BISECTION;
+        st->bisect_done = 1;
+        st->mu_x = 0.0;
+        return;
+    }
+    int best = 0;
+    double bd = fabs(vc[0] - n_elec);
+    int first_ge = P - 1;
+    for (int i = 0; i < P; i++) {
+        const double dv = fabs(vc[i] - n_elec);
+        if (dv < bd) {
+            bd = dv;
+            best = i;
+        }
+        if (vc[i] >= n_elec && i < first_ge) first_ge = i;
+    }
+    for (int i = 0; i < P; i++)
+        if (vc[i] >= n_elec) {
+            first_ge = i;
+            break;
+        }
+    const double h = (hi - lo) / (double)(P - 1);
+    if (bd <= tol_n) {
+        st->mu_x = lo + h * best;
+        st->bisect_done = 1;
+        return;
+    }
+    const double nlo = (first_ge > 0) ? lo + h * (first_ge - 1) : lo;
+    const double nhi = lo + h * first_ge;
+    st->lo = nlo;
+    st->hi = nhi;
+    if (round == last_round) {
+        st->mu_x = 0.5 * (nlo + nhi);
+        st->bisect_done = 1;
+    }
+}
+
+void launch_bisect_round(cudaStream_t st, const double *rho, const double *g, const double *mom,
+                         int M, double n_elec, double tol_n, int round, double *cand,
+                         DevState *state)
+{
+    k_bisect_round<<<kBisectCand, 256, 0, st>>>(rho, g, mom, M, n_elec, tol_n, round,
+                                                kBisectRounds - 1, cand, state);
+}
+
+// c_k(mu*) by Chebyshev-Gauss quadrature (FP64), or the step coefficients.
+__global__ void __launch_bounds__(256) k_fermi_coeffs(int M, DevState *st, double *__restrict__ c)
+{
+    __shared__ double sh[32];
+    const int k = blockIdx.x;
+    const double mu_x = st->mu_x, beta_x = st->beta_x;
+    if (threadIdx.x == 0 && k == 0) st->mu = st->a * mu_x + st->b;
+    if (beta_x > 0) {
+        const int nq = st->nq;
+        double s = 0.0;
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            const double th = kPi * (q + 0.5) / nq;
+            s += fermi(cos(th), mu_x, beta_x) * cos(k * th);
+        }
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) c[k] = (k == 0 ? 1.0 : 2.0) * s / nq;
+    } else if (threadIdx.x == 0) {
+        const double th = acos(mu_x);
+        c[k] = (k == 0) ? 1.0 - th / kPi : -2.0 * sin(k * th) / (k * kPi);
+    }
+}
+
+void launch_fermi_coeffs(cudaStream_t st, int M, DevState *state, double *c)
+{
+    k_fermi_coeffs<<<M, 256, 0, st>>>(M, state, c);
+}
+
+// diagP_i = sum_k c_k g_k d[k][i];  q_a = 2 sum_{i in a} diagP_i.
+__global__ void __launch_bounds__(256)
+    k_charges(const double *__restrict__ d, const double *__restrict__ c,
+              const double *__restrict__ g, int M, int n, int natoms, double *__restrict__ diagP,
+              double *__restrict__ q)
+{
+    extern __shared__ double wsh[];
+    for (int k = threadIdx.x; k < M; k += blockDim.x) wsh[k] = c[k] * g[k];
+    __syncthreads();
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natoms) return;
+    double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+    const double *base = d + 4 * (int64_t)a;
+    for (int k = 0; k < M; k++) {
+        const double w = wsh[k];
+        const double2 v0 = *reinterpret_cast<const double2 *>(base + (int64_t)k * n);
+        const double2 v1 = *reinterpret_cast<const double2 *>(base + (int64_t)k * n + 2);
+        p0 += w * v0.x;
+        p1 += w * v0.y;
+        p2 += w * v1.x;
+        p3 += w * v1.y;
+    }
+    if (diagP) {
+        diagP[4 * a + 0] = p0;
+        diagP[4 * a + 1] = p1;
+        diagP[4 * a + 2] = p2;
+        diagP[4 * a + 3] = p3;
+    }
+    q[a] = 2.0 * (p0 + p1 + p2 + p3);
+}
+
+// n_found = 2 sum_k c_k g_k mu_k;  E_band = 2 sum_k c_k g_k (a tr(T_k X) + b mu_k).
+__global__ void __launch_bounds__(256) k_eband(const double *__restrict__ c,
+                                               const double *__restrict__ g,
+                                               const double *__restrict__ mom, int M, DevState *st)
+{
+    __shared__ double sh[32];
+    const double a = st->a, b = st->b;
+    double ne = 0.0, eb = 0.0;
+    for (int k = threadIdx.x; k < M; k += blockDim.x) {
+        const double w = c[k] * g[k];
+        const double tx = (k == 0) ? mom[1] : 0.5 * (mom[k + 1] + mom[k - 1]);
+        ne += w * mom[k];
+        eb += w * (a * tx + b * mom[k]);
+    }
+    ne = block_sum(ne, sh);
+    eb = block_sum(eb, sh);
+    if (threadIdx.x == 0) {
+        st->n_found = 2.0 * ne;
+        st->e_band = 2.0 * eb;
+    }
+}
+
+void launch_charges(cudaStream_t st, const double *d, const double *c, const double *g,
+                    const double *mom, int M, int n, int natoms, double *diagP, double *q,
+                    DevState *state)
+{
+    const int T = 256;
+    k_charges<<<(natoms + T - 1) / T, T, sizeof(double) * M, st>>>(d, c, g, M, n, natoms, diagP, q);
+    k_eband<<<1, 256, 0, st>>>(c, g, mom, M, state);
+}
+
+// ---------------------------------------------------------------------------
+// SCC update (one CTA): residual r = q_out - q_in, convergence test, Anderson
+// mixing (D. G. Anderson, J. ACM 12, 547 (1965)) over the stored history,
+// then the new Coulomb shift V = Gamma (q_in - q0).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024)
+    k_scc_update(int natoms, const double *__restrict__ qout, double *__restrict__ qin,
+                 const double *__restrict__ q0, double *__restrict__ hq, double *__restrict__ hr,
+                 int32_t *__restrict__ meta, double beta, int history, double tol,
+                 const int32_t *__restrict__ g_rp, const int32_t *__restrict__ g_ci,
+                 const double *__restrict__ g_v, double *__restrict__ V, double *__restrict__ shift,
+                 DevState *st)
+{
+    __shared__ double sh[32];
+    __shared__ double A[kMaxHistory * kMaxHistory], rhs[kMaxHistory], gam[kMaxHistory];
+    __shared__ int s_use, s_stop;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+    // 1. residual norm
+    double mx = 0.0;
+    for (int a = tid; a < natoms; a += blockDim.x) mx = fmax(mx, fabs(qout[a] - qin[a]));
+    mx = warp_max(mx);
+    if (lane == 0) sh[w] = mx;
+    __syncthreads();
+    if (tid == 0) {
+        double m = 0.0;
+        for (int i = 0; i < nw; i++) m = fmax(m, sh[i]);
+        st->dq_max = m;
+        s_stop = 0;
+        if (!(m < 1e3)) {
+            st->status = TB_ERR_DIVERGED;
+            s_stop = 1;
+        } else if (m < tol) {
+            st->converged = 1;
+            s_stop = 1;
+        }
+    }
+    __syncthreads();
+    if (s_stop) return;
+    const int m = meta[0], head = meta[1];
+    // 2. normal equations of the Anderson least-squares problem
+    const int npair = m * (m + 1) / 2;
+    for (int pr = w; pr < npair + m; pr += nw) {
+        int i, j;
+        const bool is_rhs = pr >= npair;
+        if (is_rhs) {
+            i = pr - npair;
+            j = -1;
+        } else {
+            i = 0;
+            int rem = pr;
+            while (rem > i) {
+                rem -= i + 1;
+                i++;
+            }
+            j = rem;
+        }
+        double s = 0.0;
+        for (int a = lane; a < natoms; a += 32) {
+            const double r = qout[a] - qin[a];
+            const double di = r - hr[(int64_t)i * natoms + a];
+            const double dj = is_rhs ? r : r - hr[(int64_t)j * natoms + a];
+            s += di * dj;
+        }
+        s = warp_sum(s);
+        if (lane == 0) {
+            if (is_rhs)
+                rhs[i] = s;
+            else {
+                A[i * m + j] = s;
+                A[j * m + i] = s;
+            }
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int use = m > 0;
+        for (int i = 0; i < m; i++) A[i * m + i] *= (1.0 + 1e-10);
+        for (int k = 0; k < m && use; k++) {
+            int piv = k;
+            for (int i = k + 1; i < m; i++)
+                if (fabs(A[i * m + k]) > fabs(A[piv * m + k])) piv = i;
+            if (!(fabs(A[piv * m + k]) > 1e-300)) {
+                use = 0;
+                break;
+            }
+            if (piv != k) {
+                for (int jj = 0; jj < m; jj++) {
+                    const double t = A[k * m + jj];
+                    A[k * m + jj] = A[piv * m + jj];
+                    A[piv * m + jj] = t;
+                }
+                const double t = rhs[k];
+                rhs[k] = rhs[piv];
+                rhs[piv] = t;
+            }
+            for (int i = k + 1; i < m; i++) {
+                const double f = A[i * m + k] / A[k * m + k];
+                for (int jj = k; jj < m; jj++) A[i * m + jj] -= f * A[k * m + jj];
+                rhs[i] -= f * rhs[k];
+            }
+        }
+        if (use)
+            for (int k = m - 1; k >= 0; k--) {
+                double s = rhs[k];
+                for (int jj = k + 1; jj < m; jj++) s -= A[k * m + jj] * gam[jj];
+                gam[k] = s / A[k * m + k];
+            }
+        s_use = use;
+    }
+    __syncthreads();
+    // 3. mixed input charges; the history slot `head` takes (q_in, r)
+    const int use = s_use;
+    for (int a = tid; a < natoms; a += blockDim.x) {
+        const double qi = qin[a], r = qout[a] - qi;
+        double qb = qi, rb = r;
+        if (use)
+            for (int i = 0; i < m; i++) {
+                qb -= gam[i] * (qi - hq[(int64_t)i * natoms + a]);
+                rb -= gam[i] * (r - hr[(int64_t)i * natoms + a]);
+            }
+        if (history > 0) {
+            hq[(int64_t)head * natoms + a] = qi;
+            hr[(int64_t)head * natoms + a] = r;
+        }
+        qin[a] = qb + beta * rb;
+    }
+    __syncthreads();
+    // 4. Coulomb shift of the new input charges
+    for (int a = tid; a < natoms; a += blockDim.x) {
+        double s = 0.0;
+        for (int k = g_rp[a]; k < g_rp[a + 1]; k++) s += g_v[k] * (qin[g_ci[k]] - q0[g_ci[k]]);
+        V[a] = s;
+        shift[4 * a + 0] = s;
+        shift[4 * a + 1] = s;
+        shift[4 * a + 2] = s;
+        shift[4 * a + 3] = s;
+    }
+    if (tid == 0 && history > 0) {
+        meta[1] = (head + 1) % history;
+        meta[0] = m < history ? m + 1 : history;
+    }
+}
+
+void launch_scc_update(cudaStream_t st, DevScc &s, const double *qout, double beta, int history,
+                       double tol, double *shift, DevState *state)
+{
+    k_scc_update<<<1, 1024, 0, st>>>(s.natoms, qout, s.qin, s.q0, s.hist_q, s.hist_r, s.hist_meta,
+                                     beta, history, tol, s.rowptr, s.colidx, s.val, s.V, shift,
+                                     state);
+}
+
+void launch_build_x(cudaStream_t st, const DevMatrix &m, const double *shift, int precision,
+                    const DevState *state)
+{
+    const int64_t tot = m.nnzb * 16;
+    const int T = 256;
+    k_build_x<<<(unsigned)((tot + T - 1) / T), T, 0, st>>>(
+        m.nnzb, m.blkrow, m.colidx, m.h0, shift, state, precision == TB_PREC_FP32 ? m.x32 : nullptr,
+        precision == TB_PREC_FP64 ? m.x64 : nullptr, m.xdiag32);
+}
+
+}  // namespace tb
