@@ -197,6 +197,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--column-block", type=int, default=0)
+    ap.add_argument("--density-only", action="store_true",
+                    help="time single density evaluations (the unit profiled with ncu)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -219,6 +221,26 @@ def main():
     ctx = T.Context(M=M, kT=cfg["kT"], precision=T.PREC_FP32, device=dev,
                     column_block=args.column_block, scc_tol=cfg["scc_tol"])
     ctx.set_model(m)
+    if args.density_only:
+        for _ in range(args.warmup):
+            ctx.density()
+        torch.cuda.synchronize(dev)
+        ms = []
+        for _ in range(args.steps):
+            l2_flush(dev)
+            rep = ctx.density()["report"]
+            ms.append(rep)
+        ctx.close()
+        if rank == 0:
+            tot = sum(r["t_moments_ms"] for r in ms) / 1e3
+            b = sum(r["spmm_bytes"] for r in ms)
+            nl = sum(r["spmm_launches"] for r in ms)
+            print(json.dumps({"metric": "s per density evaluation", "value":
+                              statistics.mean(r["t_total_ms"] for r in ms) / 1e3, "unit": "s",
+                              "config": cfg, "spmm_launches": nl, "spmm_GBps": b / tot / 1e9,
+                              "avg_launch_us": tot * 1e6 / nl, "column_block": ms[-1]["column_block"],
+                              "kernel_launches": ms[-1]["kernel_launches"]}), flush=True)
+        return
 
     for _ in range(args.warmup):
         l2_flush(dev)

@@ -149,7 +149,9 @@ int ensure_work(tb_ctx *ctx)
         if (B > nround) B = nround;
     }
     const int K = (p.precision == TB_PREC_FP32) ? (M + 2) / 2 : 0;
-    const int rowgroups = (p.precision == TB_PREC_FP32) ? cheb_f32_rowgroups(m.nb) : 0;
+    const int rowgroups = (p.precision == TB_PREC_FP32)
+                              ? (ctx->sp.R > 0 ? ctx->sp.G : cheb_f32_rowgroups(m.nb))
+                              : 0;
     // quadrature capacity from the Gershgorin width of H0 with a 2x margin
     // for SCC shifts; the device flags TB_ERR_SPECTRUM if it is exceeded.
     int nq_cap = 1 << 14;
@@ -215,6 +217,87 @@ double step_bytes(const DevMatrix &m, int B, int s)
     return (double)m.nnzb * (16.0 * s + 4.0) + (double)(m.nb + 1) * 4.0 + 3.0 * m.n * (double)B * s;
 }
 
+// Row-group staging plan for k_cheb_f32_staged: the group size R is the
+// candidate with the least estimated step traffic (distinct referenced block
+// rows, weighted by wave efficiency at 256 columns) whose staging buffers
+// fit three CTAs per SM; without one the unstaged kernel is used.
+int build_stage_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::vector<int32_t> &bcol)
+{
+    StagePlan &sp = ctx->sp;
+    dfree(sp.grp_ptr);
+    dfree(sp.grp_rows);
+    dfree(sp.lcol);
+    dfree(sp.lself);
+    sp = StagePlan{};
+    const int nb = (int)brow.size() - 1;
+    int nsm = 152;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+    const size_t smem_cap = 74 * 1024;  // 3 CTAs per SM
+    double best = 1e300;
+    int bestR = 0;
+    std::vector<int32_t> mark(nb, -1);
+    for (int R : {16, 24, 32, 48, 64}) {
+        const int G = (nb + R - 1) / R;
+        int64_t tot = 0;
+        int maxU = 0, maxBlk = 0;
+        for (int g = 0; g < G; g++) {
+            const int I0 = g * R, I1 = std::min(nb, I0 + R);
+            int u = 0;
+            for (int t = brow[I0]; t < brow[I1]; t++)
+                if (mark[bcol[t]] != g) {
+                    mark[bcol[t]] = g;
+                    u++;
+                }
+            tot += u;
+            maxU = std::max(maxU, u);
+            maxBlk = std::max(maxBlk, brow[I1] - brow[I0]);
+        }
+        std::fill(mark.begin(), mark.end(), -1);
+        if (cheb_f32_staged_smem(R, maxU, maxBlk) > smem_cap) continue;
+        const int64_t ctas = (int64_t)G * 4, slots = (int64_t)nsm * 3;
+        const double eff = (double)ctas / (double)(((ctas + slots - 1) / slots) * slots);
+        const double cost = (double)(tot + 2 * nb) / eff;
+        if (cost < best) {
+            best = cost;
+            bestR = R;
+        }
+    }
+    if (bestR == 0) return TB_OK;  // unstaged fallback
+    const int R = bestR, G = (nb + R - 1) / R;
+    std::vector<int32_t> gptr(G + 1, 0), grows, lcol(bcol.size()), lself(nb);
+    int maxU = 0, maxBlk = 0;
+    for (int g = 0; g < G; g++) {
+        const int I0 = g * R, I1 = std::min(nb, I0 + R);
+        std::vector<int32_t> U;
+        for (int t = brow[I0]; t < brow[I1]; t++) U.push_back(bcol[t]);
+        std::sort(U.begin(), U.end());
+        U.erase(std::unique(U.begin(), U.end()), U.end());
+        for (int t = brow[I0]; t < brow[I1]; t++)
+            lcol[t] = (int32_t)(std::lower_bound(U.begin(), U.end(), bcol[t]) - U.begin());
+        for (int I = I0; I < I1; I++)
+            lself[I] = (int32_t)(std::lower_bound(U.begin(), U.end(), I) - U.begin());
+        grows.insert(grows.end(), U.begin(), U.end());
+        gptr[g + 1] = (int32_t)grows.size();
+        maxU = std::max(maxU, (int)U.size());
+        maxBlk = std::max(maxBlk, brow[I1] - brow[I0]);
+    }
+    TB_TRY(upload(ctx, sp.grp_ptr, gptr.data(), gptr.size()));
+    TB_TRY(upload(ctx, sp.grp_rows, grows.data(), grows.size()));
+    TB_TRY(upload(ctx, sp.lcol, lcol.data(), lcol.size()));
+    TB_TRY(upload(ctx, sp.lself, lself.data(), lself.size()));
+    const size_t smem = cheb_f32_staged_smem(R, maxU, maxBlk);
+    if (cheb_f32_staged_configure(smem) != (int)cudaSuccess) {
+        cudaGetLastError();
+        return TB_OK;  // sp.R stays 0: unstaged fallback
+    }
+    sp.R = R;
+    sp.G = G;
+    sp.maxU = maxU;
+    sp.maxBlk = maxBlk;
+    sp.totalU = (int64_t)grows.size();
+    return TB_OK;
+}
+
 std::pair<cudaEvent_t, cudaEvent_t> next_events(tb_ctx *ctx)
 {
     if (ctx->ev_used == ctx->moment_events.size()) {
@@ -261,8 +344,11 @@ int density_eval(tb_ctx *ctx, bool have_shift)
             for (int k = 0; k < w.K; k++) {
                 const int kout = k + 1;
                 const bool odd = kout & 1;
-                launch_cheb_step_f32(st, m, odd ? A : Bf, odd ? Bf : A, B, k == 0,
-                                     w.partial + (int64_t)k * w.rowgroups * B * 2, w.rowgroups);
+                double *pk = w.partial + (int64_t)k * w.rowgroups * B * 2;
+                if (ctx->sp.R > 0)
+                    launch_cheb_step_f32_staged(st, m, ctx->sp, odd ? A : Bf, odd ? Bf : A, B, k == 0, pk);
+                else
+                    launch_cheb_step_f32(st, m, odd ? A : Bf, odd ? Bf : A, B, k == 0, pk, w.rowgroups);
                 ctx->launches++;
             }
             launch_f32_finalize(st, m, w.partial, w.K, w.rowgroups, B, c0, w.d, M);
@@ -400,6 +486,11 @@ void free_all(tb_ctx *ctx)
         w.T0 = w.T1 = nullptr;
     }
     w = DevWork{};
+    dfree(ctx->sp.grp_ptr);
+    dfree(ctx->sp.grp_rows);
+    dfree(ctx->sp.lcol);
+    dfree(ctx->sp.lself);
+    ctx->sp = StagePlan{};
     if (ctx->sp2_scratch) cudaFree(ctx->sp2_scratch);
     ctx->sp2_scratch = nullptr;
 }
@@ -624,6 +715,7 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
     TB_TRY(upload(ctx, m.h0diag, h0diag.data(), h0diag.size()));
     TB_TRY(upload(ctx, m.radius, radius.data(), radius.size()));
     TB_TRY(dalloc(ctx, m.xdiag32, (size_t)n));
+    TB_TRY(build_stage_plan(ctx, brow, bcol));
     // quadrature capacity: host Gershgorin width of H0, 2x margin for shifts
     double mn = 1e300, mx = -1e300;
     for (int i = 0; i < n; i++) {

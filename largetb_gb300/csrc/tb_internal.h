@@ -50,6 +50,16 @@ struct DevMatrix {
     float *xdiag32 = nullptr;    // n, diagonal of the FP32 X actually used
 };
 
+// Row-group staging plan of the FP32 step kernel (see k_cheb_f32_staged).
+struct StagePlan {
+    int32_t R = 0, G = 0, maxU = 0, maxBlk = 0;
+    int64_t totalU = 0;
+    int32_t *grp_ptr = nullptr;   // G+1
+    int32_t *grp_rows = nullptr;  // totalU distinct block rows per group
+    int32_t *lcol = nullptr;      // nnzb: local index of colidx[t] in its group's list
+    int32_t *lself = nullptr;     // nb: local index of block row I in its own group's list
+};
+
 struct DevScc {
     int32_t natoms = 0;
     int64_t nnz = 0;
@@ -95,6 +105,7 @@ struct tb_ctx {
     tb::DevMatrix m;
     tb::DevScc s;
     tb::DevWork w;
+    tb::StagePlan sp;
     int64_t launches = 0;
     int64_t spmm_launches = 0;
     double spmm_bytes = 0.0;
@@ -125,6 +136,11 @@ void launch_cheb_step_f64(cudaStream_t st, const DevMatrix &m, const double *Tin
 void launch_cheb_step_f32(cudaStream_t st, const DevMatrix &m, const float *Tin, float *Tout,
                           int B, int first, double *partial_k, int rowgroups);
 int cheb_f32_rowgroups(int nb);
+size_t cheb_f32_staged_smem(int R, int maxU, int maxBlk);
+int cheb_f32_staged_configure(size_t smem);  // returns a cudaError_t
+int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const StagePlan &sp,
+                                const float *Tin, float *Tout, int B, int first,
+                                double *partial_k);
 void launch_f32_finalize(cudaStream_t st, const DevMatrix &m, const double *partial, int K,
                          int rowgroups, int B, int c0, double *d, int M);
 void launch_moment_sums(cudaStream_t st, const double *d, int n, int nmom, double *mom);

@@ -426,6 +426,166 @@ void launch_cheb_step_f32(cudaStream_t st, const DevMatrix &m, const float *Tin,
                                                 first, partial_k);
 }
 
+// ---------------------------------------------------------------------------
+// FP32 Chebyshev step, staged form.  Block rows are cut into groups of R
+// consecutive rows; for each group the host lists U_g, the distinct block
+// rows its blocks reference (for beta-cristobalite in cell order, |U_g| is
+// about 1.6 R against 3.67 R block reads without staging).  A CTA takes one
+// group x 64 columns and copies, with 16-byte cp.async (LDGSTS), the U_g rows
+// of T_k, its own rows of T_{k-1} and its X blocks into shared memory, then
+// every warp computes its block rows from shared memory: lane = 2 columns.
+// Column dot products as in k_cheb_f32, one FP64 pair per column per CTA.
+// ---------------------------------------------------------------------------
+constexpr int kV2Cols = 64;
+constexpr int kV2Warps = 8;
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src)
+{
+    // no memory clobber: the copies are ordered by cp_async_wait_all below
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src));
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+__global__ void __launch_bounds__(32 * kV2Warps)
+    k_cheb_f32_staged(int nb, int R, const int32_t *__restrict__ rowptr,
+                      const int32_t *__restrict__ lcol, const int32_t *__restrict__ lself,
+                      const int32_t *__restrict__ grp_ptr, const int32_t *__restrict__ grp_rows,
+                      const float *__restrict__ x32, const float *__restrict__ Tin,
+                      float *__restrict__ Tout, int B, int first, double *__restrict__ partial_k,
+                      int maxU, int maxBlk)
+{
+    extern __shared__ float4 smem4[];
+    float *sT = reinterpret_cast<float *>(smem4);  // maxU*4 rows x 64
+    float *sP = sT + maxU * 4 * kV2Cols;            // R*4 rows x 64 (T_{k-1})
+    float *sX = sP + R * 4 * kV2Cols;               // maxBlk*16
+    int *sU = reinterpret_cast<int *>(sX + maxBlk * 16);  // maxU block rows
+    int *sL = sU + maxU;                                  // maxBlk local columns
+    int *sR = sL + maxBlk;                                // R+1 row offsets
+    const int g = blockIdx.x, chunk = blockIdx.y, tid = threadIdx.x;
+    const int I0 = g * R;
+    const int I1 = min(nb, I0 + R);
+    const int nr = I1 - I0;
+    const int u0 = grp_ptr[g], nu = grp_ptr[g + 1] - u0;
+    const int tb0 = rowptr[I0], nbk = rowptr[I1] - tb0;
+    const int col0 = chunk * kV2Cols;
+    // ---- indices first, so every copy address below comes from shared memory ----
+    for (int i = tid; i < nu; i += blockDim.x) sU[i] = grp_rows[u0 + i];
+    for (int i = tid; i < nbk; i += blockDim.x) sL[i] = lcol[tb0 + i];
+    for (int i = tid; i <= nr; i += blockDim.x) sR[i] = rowptr[I0 + i] - tb0;
+    for (int idx = tid; idx < nbk * 4; idx += blockDim.x)
+        cp_async16(sX + idx * 4, x32 + (int64_t)tb0 * 16 + idx * 4);
+    if (!first)
+        for (int idx = tid; idx < nr * 64; idx += blockDim.x) {
+            const int r = idx >> 6, m = (idx >> 4) & 3, sg = idx & 15;
+            cp_async16(sP + (r * 4 + m) * kV2Cols + sg * 4,
+                       Tout + (int64_t)(4 * (I0 + r) + m) * B + col0 + sg * 4);
+        }
+    __syncthreads();
+    // ---- stage T_k rows: 16 segments of 16 bytes per 64-column row ----
+    for (int idx = tid; idx < nu * 64; idx += blockDim.x) {
+        const int u = idx >> 6, m = (idx >> 4) & 3, sg = idx & 15;
+        cp_async16(sT + (u * 4 + m) * kV2Cols + sg * 4,
+                   Tin + (int64_t)(4 * sU[u] + m) * B + col0 + sg * 4);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // ---- compute ----
+    const int lane = tid & 31, w = tid >> 5, c = 2 * lane;
+    double see[2] = {0.0, 0.0}, seo[2] = {0.0, 0.0};
+    for (int r = w; r < nr; r += kV2Warps) {
+        const int I = I0 + r;
+        const int ta = sR[r], te = sR[r + 1];
+        float acc[4][2];
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[q][0] = acc[q][1] = 0.f;
+        for (int t = ta; t < te; t++) {
+            const float *tv = sT + sL[t] * 4 * kV2Cols + c;
+            const float4 *xb = reinterpret_cast<const float4 *>(sX + t * 16);
+            float2 v[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) v[m] = *reinterpret_cast<const float2 *>(tv + m * kV2Cols);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float4 xr = xb[q];
+                const float xm[4] = {xr.x, xr.y, xr.z, xr.w};
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    acc[q][0] = fmaf(xm[m], v[m].x, acc[q][0]);
+                    acc[q][1] = fmaf(xm[m], v[m].y, acc[q][1]);
+                }
+            }
+        }
+        const float *own = sT + lself[I] * 4 * kV2Cols + c;
+        float ee[2] = {0.f, 0.f}, eo[2] = {0.f, 0.f};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float2 ov = *reinterpret_cast<const float2 *>(own + q * kV2Cols);
+            float2 o;
+            if (first) {
+                o = make_float2(acc[q][0], acc[q][1]);
+            } else {
+                const float2 p = *reinterpret_cast<const float2 *>(sP + (r * 4 + q) * kV2Cols + c);
+                o.x = 2.f * acc[q][0] - p.x;
+                o.y = 2.f * acc[q][1] - p.y;
+            }
+            *reinterpret_cast<float2 *>(Tout + (int64_t)(4 * I + q) * B + col0 + c) = o;
+            ee[0] = fmaf(ov.x, ov.x, ee[0]);
+            ee[1] = fmaf(ov.y, ov.y, ee[1]);
+            eo[0] = fmaf(ov.x, o.x, eo[0]);
+            eo[1] = fmaf(ov.y, o.y, eo[1]);
+        }
+        see[0] += (double)ee[0];
+        see[1] += (double)ee[1];
+        seo[0] += (double)eo[0];
+        seo[1] += (double)eo[1];
+    }
+    __syncthreads();  // shared T no longer needed: reuse for the reduction
+    double *red = reinterpret_cast<double *>(smem4);  // [8][64][2]
+    red[(w * kV2Cols + c) * 2 + 0] = see[0];
+    red[(w * kV2Cols + c) * 2 + 1] = seo[0];
+    red[(w * kV2Cols + c + 1) * 2 + 0] = see[1];
+    red[(w * kV2Cols + c + 1) * 2 + 1] = seo[1];
+    __syncthreads();
+    if (tid < 2 * kV2Cols) {
+        const int j = tid >> 1, which = tid & 1;
+        double sacc = 0.0;
+#pragma unroll
+        for (int q = 0; q < kV2Warps; q++) sacc += red[(q * kV2Cols + j) * 2 + which];
+        partial_k[((int64_t)g * B + col0 + j) * 2 + which] = sacc;
+    }
+}
+
+int cheb_f32_staged_configure(size_t smem)
+{
+    return (int)cudaFuncSetAttribute(k_cheb_f32_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+}
+
+size_t cheb_f32_staged_smem(int R, int maxU, int maxBlk)
+{
+    size_t b = (size_t)(maxU * 4 * kV2Cols + R * 4 * kV2Cols + maxBlk * 16) * sizeof(float) +
+               (size_t)(maxU + maxBlk + R + 1) * sizeof(int);
+    const size_t red = (size_t)kV2Warps * kV2Cols * 2 * sizeof(double);
+    return b > red ? b : red;
+}
+
+int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const StagePlan &sp,
+                                const float *Tin, float *Tout, int B, int first,
+                                double *partial_k)
+{
+    const size_t smem = cheb_f32_staged_smem(sp.R, sp.maxU, sp.maxBlk);
+    dim3 grid(sp.G, B / kV2Cols);
+    k_cheb_f32_staged<<<grid, 32 * kV2Warps, smem, st>>>(m.nb, sp.R, m.rowptr, sp.lcol, sp.lself,
+                                                         sp.grp_ptr, sp.grp_rows, m.x32, Tin,
+                                                         Tout, B, first, partial_k, sp.maxU,
+                                                         sp.maxBlk);
+    return 1;
+}
+
 // Sum the per-rowgroup partials of a slab and turn them into moments:
 // d[2k][j] = 2 <T_k,T_k>_j - 1,  d[2k+1][j] = 2 <T_k,T_{k+1}>_j - X_jj.
 __global__ void k_f32_finalize(const double *__restrict__ partial, int K, int rowgroups, int B,
