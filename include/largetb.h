@@ -195,6 +195,33 @@ const char *tb_status_string(int status);
 int tb_abi_version(void);
 
 /* ------------------------------------------------------------------------ */
+/* Allocation-free variant                                                   */
+/* ------------------------------------------------------------------------ */
+/* No counterpart in the reference: an entry point for callers that cannot
+ * allocate device memory -- codes whose device memory belongs to their own
+ * pool or allocator, or that run under a fixed memory budget.  It computes
+ * the exact-trace moments mu_k = tr T_k(X), k = 0..M (the `moments` output
+ * of tb_density) of X = (H - b I)/a for a CSR matrix H (n x n, any pattern,
+ * FP64) that is already in device memory, and allocates nothing: the
+ * recurrence's scratch is a static device array of 2 x TB_NOALLOC_MAX_N x 64
+ * doubles (8 MiB) that every GPU loading this library holds until the
+ * process exits.  d_rowptr (n+1), d_colidx and d_vals (nnz) and d_moments
+ * (M+1) are device pointers owned by the caller; d_moments is cleared and
+ * overwritten.  `stream` is a cudaStream_t (NULL: the legacy default stream);
+ * the call returns after the stream has finished the work.
+ *   - The first call on a device looks up the scratch array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - Every call shares the one scratch array: calls that overlap on the GPU
+ *     (from several host threads or streams) race and give wrong results.
+ *   - n > TB_NOALLOC_MAX_N returns TB_ERR_UNSUPPORTED without touching the
+ *     GPU; bad arguments return TB_ERR_INVALID_ARG. */
+#define TB_NOALLOC_MAX_N 8192
+int tb_moments_noalloc(int32_t n, const int32_t *d_rowptr, const int32_t *d_colidx,
+                       const double *d_vals, double a, double b, int32_t M, double *d_moments,
+                       void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Model builder: upstream of the boundary.  Builds what the reference's     */
 /* arrangeCoordinates/constructH/initializeForSCF produce, for synthetic     */
 /* inputs: the reference's alpha-quartz cell, or beta-cristobalite.          */
