@@ -895,11 +895,28 @@ int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, do
 
 int tb_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep)
 {
-    (void)diagP;
-    (void)q;
-    (void)e_band;
-    (void)rep;
-    return fail(ctx, TB_ERR_UNSUPPORTED, "SP2 not built yet");
+    if (!ctx) return TB_ERR_INVALID_ARG;
+    if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian not set");
+    if (!(ctx->p.n_electrons > 0))
+        return fail(ctx, TB_ERR_NOT_READY, "n_electrons unset (give it in tb_params or tb_set_scc)");
+    TB_TRY(set_device(ctx));
+    cudaEvent_t e0;
+    begin_call(ctx, &e0);
+    tb_report r;
+    std::memset(&r, 0, sizeof(r));
+    const int rc = run_sp2(ctx, diagP, q, e_band, &r, nullptr, 0);
+    cudaEvent_t e1;
+    cudaEventCreate(&e1);
+    cudaEventRecord(e1, ctx->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    r.t_total_ms = ms;
+    r.asym_max = ctx->asym_max;
+    if (rep) *rep = r;
+    return rc;
 }
 
 int tb_kpm_dos(tb_ctx *ctx, int32_t n_moments, int32_t n_random, uint64_t seed, int32_t npts,

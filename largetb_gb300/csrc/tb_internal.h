@@ -156,4 +156,10 @@ void launch_charges(cudaStream_t st, const double *d, const double *c, const dou
 void launch_scc_update(cudaStream_t st, DevScc &s, const double *qout, double beta, int history,
                        double tol, double *shift, DevState *state);
 
+// ---- tb_sp2.cu ----------------------------------------------------------
+// SP2 purification of the context's H; branches_out (optional) receives the
+// applied branch sequence (-1: X^2, +1: 2X - X^2).
+int run_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep,
+            int32_t *branches_out, int32_t branches_cap);
+
 }  // namespace tb

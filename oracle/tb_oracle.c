@@ -1070,9 +1070,8 @@ int orc_sp2(int n, const int32_t *rowptr, const int32_t *col, const double *val,
 
     int it;
     double prev1 = INFINITY, prev2 = INFINITY;
-    int nth = p->nthreads > 0 ? p->nthreads : 1;
 #ifdef _OPENMP
-    omp_set_num_threads(nth);
+    if (p->nthreads > 0) omp_set_num_threads(p->nthreads);
 #endif
     for (it = 0;; it++) {
         /* X^2 row by row (exact), idempotency error and traces. */
@@ -1137,7 +1136,10 @@ int orc_sp2(int n, const int32_t *rowptr, const int32_t *col, const double *val,
         int stop = 0;
         if (idem < p->idem_tol) stop = 1;
         if (p->trace_tol > 0 && fabs(2.0 * trX - p->n_elec) < p->trace_tol && idem < 1.0) stop = 1;
-        if (it >= 4 && idem >= prev2) stop = 1;
+        /* stagnation: past the oscillating start (errors below 0.1, where the
+         * expansion converges quadratically) an error that no longer falls
+         * over two steps has reached the drop-tolerance / round-off floor */
+        if (it >= 2 && prev2 < 0.1 && idem >= prev2) stop = 1;
         if (it >= p->max_iter) stop = 1;
         if (stop) {
             R.idem_err = idem;

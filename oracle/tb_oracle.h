@@ -227,7 +227,10 @@ typedef struct {
  * 2 tr X > N_e else 2X - X^2 (branch rule of computeAlphas,
  * withSP2.cpp:1027-1030; recursion getSP2, withSP2.cpp:956-984).
  * branches (length max_iter, may be NULL) receives -1 for X^2, +1 for 2X-X^2;
- * idem_hist receives ||X^2-X||_F before each step. */
+ * idem_hist receives ||X^2-X||_F before each step.  Stops when the error is
+ * below idem_tol, when (after the oscillating start, errors < 0.1) it fails
+ * to fall over two steps, or at max_iter; returns the last X whose error
+ * was measured. */
 int orc_sp2(int n, const int32_t *rowptr, const int32_t *col, const double *val,
             const int32_t *orb2atom, int natoms, const orc_sp2_params *p, double *diagP,
             double *q, int32_t *branches, double *idem_hist, double *trace_hist,

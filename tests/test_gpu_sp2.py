@@ -1,0 +1,67 @@
+"""SP2 block SpGEMM (tb_sp2) against the FP64 CPU oracle's SP2.
+
+Both run the same recursion: X_0 from Gershgorin, the reference's branch
+rule (X^2 if 2 tr X > N_e, else 2X - X^2), 4x4 blocks dropped below the drop
+tolerance, the same stopping rule.  FP64 blocks agree with the oracle up to
+summation order (charges 1e-8 e without dropping); FP32 blocks stop at their
+own idempotency floor, held to charges within 1e-4 e.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(nx, ny, nz, sigma=0.08, seed=3003):
+    import largetb_gb300 as T
+    return (T.model_cristobalite(nx, ny, nz, sigma_ang=sigma, seed=seed),
+            O.cristobalite(nx, ny, nz, sigma_ang=sigma, seed=seed))
+
+
+def _run(T, m, prec, drop=1e-5, max_iter=40):
+    with T.Context(precision=prec, sp2_drop_tol=drop, sp2_max_iter=max_iter,
+                   sp2_idem_tol=1e-10) as c:
+        c.set_model(m)
+        return c.sp2()
+
+
+@pytest.mark.parametrize("drop", [0.0, 1e-5])
+def test_sp2_fp64_matches_oracle(gpu, drop):
+    m, o = _pair(2, 2, 2)
+    ref = O.sp2(o, drop_tol=drop, max_iter=40, idem_tol=1e-10)
+    r = _run(gpu, m, gpu.PREC_FP64, drop)
+    rep = r["report"]
+    assert rep["sp2_iters"] == ref["iters"]
+    assert np.abs(r["q"] - ref["q"]).max() < 1e-8
+    assert abs(r["e_band"] - ref["e_band"]) < 1e-7
+    assert abs(rep["idem_err"] - ref["idem_err"]) < 1e-8
+    assert rep["sp2_nnzb"] == ref["nnzb"]
+
+
+def test_sp2_fp32_matches_oracle(gpu):
+    m, o = _pair(2, 2, 2)
+    ref = O.sp2(o, drop_tol=1e-5, max_iter=40, idem_tol=1e-10)
+    r = _run(gpu, m, gpu.PREC_FP32)
+    rep = r["report"]
+    assert abs(rep["sp2_iters"] - ref["iters"]) <= 3
+    assert rep["idem_err"] < 1e-3
+    assert np.abs(r["q"] - ref["q"]).max() < 1e-4
+    assert abs(r["q"].sum() - m.n_electrons) < 1e-3
+    assert abs(r["e_band"] - ref["e_band"]) / m.natoms < 1e-5
+
+
+def test_sp2_full_size_4x4x4(gpu):
+    """1536 atoms, 6144 orbitals, sigma 0.08 A, drop 1e-5, <= 40 steps."""
+    m, o = _pair(4, 4, 4)
+    ref = O.sp2(o, drop_tol=1e-5, max_iter=40, idem_tol=1e-10)
+    r64 = _run(gpu, m, gpu.PREC_FP64)
+    r32 = _run(gpu, m, gpu.PREC_FP32)
+    assert abs(r64["report"]["sp2_iters"] - ref["iters"]) <= 1
+    assert np.abs(r64["q"] - ref["q"]).max() < 1e-4
+    assert abs(r64["report"]["sp2_nnzb"] - ref["nnzb"]) <= 0.01 * ref["nnzb"]
+    assert np.abs(r32["q"] - r64["q"]).max() < 1e-3
+    for r in (r64, r32):
+        assert abs(r["q"].sum() - m.n_electrons) < 1e-2
+        assert r["report"]["idem_err"] < 1e-2
