@@ -922,15 +922,37 @@ int tb_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep
 int tb_kpm_dos(tb_ctx *ctx, int32_t n_moments, int32_t n_random, uint64_t seed, int32_t npts,
                double *moments, double *energies, double *dos, tb_report *rep)
 {
-    (void)n_moments;
-    (void)n_random;
-    (void)seed;
-    (void)npts;
-    (void)moments;
-    (void)energies;
-    (void)dos;
-    (void)rep;
-    return fail(ctx, TB_ERR_UNSUPPORTED, "stochastic DOS not built yet");
+    if (!ctx) return TB_ERR_INVALID_ARG;
+    if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian not set");
+    if (n_moments < 2 || n_moments > 100000 || n_random < 1 || n_random > 4096 || npts < 1 ||
+        !moments || !energies || !dos)
+        return fail(ctx, TB_ERR_INVALID_ARG,
+                    "need 2 <= n_moments <= 100000, 1 <= n_random <= 4096, npts >= 1, outputs");
+    TB_TRY(set_device(ctx));
+    cudaEvent_t e0;
+    begin_call(ctx, &e0);
+    double a = 0.0, b = 0.0;
+    int64_t nl = 0;
+    const int rc = run_kpm_dos(ctx, n_moments, n_random, seed, npts, moments, energies, dos, &a, &b, &nl);
+    cudaEvent_t e1;
+    cudaEventCreate(&e1);
+    cudaEventRecord(e1, ctx->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rep) {
+        std::memset(rep, 0, sizeof(*rep));
+        rep->a = a;
+        rep->b = b;
+        rep->lmin = b - a;
+        rep->lmax = b + a;
+        rep->t_total_ms = ms;
+        rep->kernel_launches = nl;
+        rep->precision = TB_PREC_FP64;
+    }
+    return rc;
 }
 
 }  // extern "C"

@@ -162,4 +162,8 @@ void launch_scc_update(cudaStream_t st, DevScc &s, const double *qout, double be
 int run_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep,
             int32_t *branches_out, int32_t branches_cap);
 
+// ---- tb_dos.cu ----------------------------------------------------------
+int run_kpm_dos(tb_ctx *ctx, int nmom, int nr, uint64_t seed, int npts, double *mom, double *E,
+                double *dos, double *a_out, double *b_out, int64_t *launches);
+
 }  // namespace tb
