@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(workload="beta-cristobalite 6x6x6 SCC solve", cells=[6, 6, 6], atoms=5184,
                 orbitals=20736, sigma_ang=0.05, seed=2002, M=400, kT=0.01, scc_tol=1e-6,
-                cutoff_bohr=4.0, mixer="anderson(8, 0.2)", trace="exact, all identity columns")
+                cutoff_bohr=4.0, mixer="anderson(12, 0.2)", trace="exact, all identity columns")
 METRIC = "s per converged SCC solve (5184 atoms, |dq|<1e-6 e)"
 
 

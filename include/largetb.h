@@ -73,7 +73,10 @@ typedef struct tb_params {
     double kT;             /* electronic temperature, Hartree; <= 0 selects the step
                               function of getKPE (withSP2_deltaH.cpp:1100-1103) */
     double n_electrons;    /* electrons, both spins; <= 0 takes sum(q0) from tb_set_scc */
-    int32_t column_block;  /* identity columns per slab; 0 = autotune */
+    int32_t column_block;  /* identity columns per slab (multiple of 128), or 0: on the
+                              first density evaluation of a matrix, time a few
+                              Chebyshev steps of every kernel/width candidate and
+                              keep the cheapest per column */
     int32_t device;        /* CUDA device ordinal */
     double spectral_pad;   /* relative widening of the Gershgorin interval */
     double mu_tol;         /* bisection tolerance on the electron count */
@@ -114,7 +117,7 @@ typedef struct tb_report {
 
 typedef struct tb_ctx tb_ctx;
 
-/* Fill *p with defaults (M = 200, Jackson, kT = 0.01, FP64, Anderson 8 / 0.2,
+/* Fill *p with defaults (M = 200, Jackson, kT = 0.01, FP64, Anderson 12 / 0.2,
  * scc_tol = 1e-6, SP2 drop 1e-5 / 40 iterations). */
 int tb_params_init(tb_params *p);
 

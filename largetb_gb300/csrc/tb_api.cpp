@@ -135,6 +135,99 @@ int set_device(tb_ctx *ctx)
     return TB_OK;
 }
 
+double step_bytes(const DevMatrix &m, int B, int s);
+
+// Slab-width autotuner (column_block = 0): time kTuneSteps Chebyshev steps of
+// one slab for every candidate kernel/width on this matrix and keep the one
+// with the least time per identity column.  Runs once per matrix and
+// precision; the X used is the unshifted one.
+int autotune(tb_ctx *ctx)
+{
+    constexpr int kTuneSteps = 12;
+    DevMatrix &m = ctx->m;
+    cudaStream_t st = ctx->stream;
+    const int prec = ctx->p.precision;
+    const int nround = ((m.n + 63) / 64) * 64;
+    struct Cand {
+        bool persist;
+        int B;
+    };
+    std::vector<Cand> cands;
+    if (prec == TB_PREC_FP32) {
+        if (ctx->pp.R > 0) cands.push_back({true, ctx->pp.B});
+        for (int B : {256, 384, 512})
+            if (B <= ((m.n + 127) / 128) * 128 || B == 256) cands.push_back({false, std::min(B, ((m.n + 127) / 128) * 128)});
+    } else {
+        for (int B : {64, 128, 256})
+            if (B <= nround || B == 64) cands.push_back({false, std::min(B, ((m.n + 63) / 64) * 64)});
+    }
+    DevState *state = nullptr;
+    TB_TRY(dalloc(ctx, state, 1));
+    if (prec == TB_PREC_FP32 && !m.x32) TB_TRY(dalloc(ctx, m.x32, (size_t)m.nnzb * 16));
+    if (prec == TB_PREC_FP64 && !m.x64) TB_TRY(dalloc(ctx, m.x64, (size_t)m.nnzb * 16));
+    launch_gershgorin(st, m, nullptr, 0.0, 0.0, 2, 1 << 22, state);
+    launch_build_x(st, m, nullptr, prec, state);
+    double best = 1e300;
+    Cand pick = cands.front();
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    for (const Cand &cd : cands) {
+        const int B = cd.B;
+        const size_t es = prec == TB_PREC_FP32 ? 4 : 8;
+        const int rowgroups = cd.persist ? ctx->pp.G : (ctx->sp.R > 0 ? ctx->sp.G : cheb_f32_rowgroups(m.nb));
+        char *T0 = nullptr, *T1 = nullptr;
+        double *part = nullptr, *dd = nullptr;
+        TB_TRY(dalloc(ctx, T0, (size_t)m.n * B * es));
+        TB_TRY(dalloc(ctx, T1, (size_t)m.n * B * es));
+        if (prec == TB_PREC_FP32)
+            TB_TRY(dalloc(ctx, part, (size_t)(kTuneSteps + 1) * rowgroups * B * 2));
+        else
+            TB_TRY(dalloc(ctx, dd, (size_t)(kTuneSteps + 2) * m.n));
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; rep++) {  // the first pass warms up
+            cudaEventRecord(a, st);
+            if (cd.persist) {
+                cudaMemsetAsync(ctx->pp.flags, 0, sizeof(int32_t) * ctx->pp.G * ctx->pp.nc, st);
+                launch_cheb_f32_persistent(st, m, ctx->pp, kTuneSteps, B, 0, (float *)T0, (float *)T1, part,
+                                           ctx->pp.flags, ctx->pp.err);
+            } else {
+                launch_slab_identity(st, T0, m.n, B, 0, prec);
+                for (int k = 0; k < kTuneSteps; k++) {
+                    const bool odd = (k + 1) & 1;
+                    char *in = odd ? T0 : T1, *out = odd ? T1 : T0;
+                    if (prec == TB_PREC_FP64)
+                        launch_cheb_step_f64(st, m, (double *)in, (double *)out, B, 0, k == 0, dd, k + 1);
+                    else if (ctx->sp.R > 0)
+                        launch_cheb_step_f32_staged(st, m, ctx->sp, (float *)in, (float *)out, B, k == 0,
+                                                    part + (int64_t)k * rowgroups * B * 2);
+                    else
+                        launch_cheb_step_f32(st, m, (float *)in, (float *)out, B, k == 0,
+                                             part + (int64_t)k * rowgroups * B * 2, rowgroups);
+                }
+            }
+            cudaEventRecord(b, st);
+            TB_CUDA(cudaEventSynchronize(b));
+            cudaEventElapsedTime(&ms, a, b);
+        }
+        TB_CUDA(cudaGetLastError());
+        const double per_col = ms / (double)std::min(B, m.n);
+        if (per_col < best) {
+            best = per_col;
+            pick = cd;
+        }
+        dfree(T0);
+        dfree(T1);
+        dfree(part);
+        dfree(dd);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    dfree(state);
+    ctx->tuned[prec] = pick.persist ? -1 : pick.B;
+    return TB_OK;
+}
+
 // Work buffers sized for the current parameters and matrix.
 int ensure_work(tb_ctx *ctx)
 {
@@ -142,22 +235,31 @@ int ensure_work(tb_ctx *ctx)
     const DevMatrix &m = ctx->m;
     const tb_params &p = ctx->p;
     const int M = p.M;
+    if (p.column_block == 0 && ctx->tuned[p.precision] == 0) TB_TRY(autotune(ctx));
+    const int tuned = ctx->tuned[p.precision];
+    const bool persist = p.precision == TB_PREC_FP32 && ctx->pp.R > 0 && p.column_block == 0 && tuned < 0;
     int B = p.column_block;
-    if (B == 0) B = (p.precision == TB_PREC_FP32) ? 256 : 128;
-    {
-        const int nround = ((m.n + 127) / 128) * 128;
+    if (persist)
+        B = ctx->pp.B;
+    else {
+        if (B == 0) B = tuned > 0 ? tuned : ((p.precision == TB_PREC_FP32) ? 256 : 128);
+        // the unstaged FP32 kernel works in 128-column chunks, the others in 64
+        const int q = (p.precision == TB_PREC_FP32 && ctx->sp.R == 0) ? 128 : 64;
+        const int nround = ((m.n + q - 1) / q) * q;
         if (B > nround) B = nround;
     }
     const int K = (p.precision == TB_PREC_FP32) ? (M + 2) / 2 : 0;
     const int rowgroups = (p.precision == TB_PREC_FP32)
-                              ? (ctx->sp.R > 0 ? ctx->sp.G : cheb_f32_rowgroups(m.nb))
+                              ? (persist ? ctx->pp.G : (ctx->sp.R > 0 ? ctx->sp.G : cheb_f32_rowgroups(m.nb)))
                               : 0;
+    w.persist = persist;
     // quadrature capacity from the Gershgorin width of H0 with a 2x margin
     // for SCC shifts; the device flags TB_ERR_SPECTRUM if it is exceeded.
     int nq_cap = 1 << 14;
     if (p.kT > 0)
         nq_cap = std::max(nq_cap, quad_nodes(M, 2.0 * (ctx->h0_lmax - ctx->h0_lmin) / p.kT));
     const bool same = w.M == M && w.B == B && w.K == K && w.precision == p.precision &&
+                      w.persist == persist &&
                       w.rowgroups == rowgroups && w.nq_cap >= nq_cap && w.d && w.mom && w.T0 &&
                       w.kernel == p.kernel;
     if (same) return TB_OK;
@@ -298,6 +400,113 @@ int build_stage_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::v
     return TB_OK;
 }
 
+// Task plan of the persistent FP32 kernel: row groups of R block rows, each
+// with its halo (referenced rows owned by other groups) and its neighbouring
+// groups; nc 64-column chunks per slab so that all G * nc tasks are resident
+// together (a requirement of the cooperative launch).  R minimises
+// slabs x tasks per SM x (R + mean halo); without a fitting R the per-step
+// kernels are used.
+int build_persist_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::vector<int32_t> &bcol)
+{
+    PersistPlan &pp = ctx->pp;
+    dfree(pp.lcode);
+    dfree(pp.hptr);
+    dfree(pp.hrows);
+    dfree(pp.nptr);
+    dfree(pp.ngrp);
+    dfree(pp.flags);
+    dfree(pp.err);
+    pp = PersistPlan{};
+    const int nb = (int)brow.size() - 1, n = 4 * nb;
+    int nsm = 152, coop = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+    if (!coop) return TB_OK;
+    struct Cand {
+        int R, G, nc, B, maxH, maxBlk, maxNG;
+        double cost;
+    };
+    Cand best{0, 0, 0, 0, 0, 0, 0, 1e300};
+    for (int R : {16, 24, 32, 48, 64}) {  // kernel instances for 2, 3, 4, 6, 8 rows per warp
+        const int G = (nb + R - 1) / R;
+        int maxH = 0, maxBlk = 0, maxNG = 0;
+        int64_t totH = 0;
+        for (int g = 0; g < G; g++) {
+            const int I0 = g * R, I1 = std::min(nb, I0 + R);
+            std::vector<int32_t> halo, ng;
+            for (int t = brow[I0]; t < brow[I1]; t++)
+                if (bcol[t] < I0 || bcol[t] >= I1) halo.push_back(bcol[t]);
+            std::sort(halo.begin(), halo.end());
+            halo.erase(std::unique(halo.begin(), halo.end()), halo.end());
+            for (int J : halo) ng.push_back(J / R);
+            ng.erase(std::unique(ng.begin(), ng.end()), ng.end());
+            maxH = std::max(maxH, (int)halo.size());
+            maxNG = std::max(maxNG, (int)ng.size());
+            maxBlk = std::max(maxBlk, brow[I1] - brow[I0]);
+            totH += (int64_t)halo.size();
+        }
+        const size_t smem = cheb_f32_persistent_smem(R, maxH, maxBlk, maxNG);
+        if (smem > 227 * 1024) continue;
+        int per_sm = 0;
+        if (cheb_f32_persistent_setup(R, smem, &per_sm) != (int)cudaSuccess || per_sm < 1) {
+            cudaGetLastError();
+            continue;
+        }
+        const int64_t slots = (int64_t)nsm * per_sm;
+        int nc = (int)std::min<int64_t>(slots / G, (n + 63) / 64);
+        if (nc < 1) continue;
+        const int B = 64 * nc, nslab = (n + B - 1) / B;
+        const double tasks_per_sm = std::ceil((double)G * nc / nsm);
+        const double cost = (double)nslab * tasks_per_sm * (R + (double)totH / G);
+        if (cost < best.cost) best = Cand{R, G, nc, B, maxH, maxBlk, maxNG, cost};
+    }
+    if (best.R == 0) return TB_OK;
+    const int R = best.R, G = best.G;
+    std::vector<int32_t> lcode(bcol.size()), hptr(G + 1, 0), hrows, nptr(G + 1, 0), ngrp;
+    for (int g = 0; g < G; g++) {
+        const int I0 = g * R, I1 = std::min(nb, I0 + R);
+        std::vector<int32_t> halo;
+        for (int t = brow[I0]; t < brow[I1]; t++)
+            if (bcol[t] < I0 || bcol[t] >= I1) halo.push_back(bcol[t]);
+        std::sort(halo.begin(), halo.end());
+        halo.erase(std::unique(halo.begin(), halo.end()), halo.end());
+        for (int t = brow[I0]; t < brow[I1]; t++) {
+            const int J = bcol[t];
+            lcode[t] = (J >= I0 && J < I1)
+                           ? J - I0
+                           : R + (int32_t)(std::lower_bound(halo.begin(), halo.end(), J) - halo.begin());
+        }
+        std::vector<int32_t> ng;
+        for (int J : halo) ng.push_back(J / R);
+        ng.erase(std::unique(ng.begin(), ng.end()), ng.end());
+        hrows.insert(hrows.end(), halo.begin(), halo.end());
+        ngrp.insert(ngrp.end(), ng.begin(), ng.end());
+        hptr[g + 1] = (int32_t)hrows.size();
+        nptr[g + 1] = (int32_t)ngrp.size();
+    }
+    if (hrows.empty()) hrows.push_back(0);
+    if (ngrp.empty()) ngrp.push_back(0);
+    TB_TRY(upload(ctx, pp.lcode, lcode.data(), lcode.size()));
+    TB_TRY(upload(ctx, pp.hptr, hptr.data(), hptr.size()));
+    TB_TRY(upload(ctx, pp.hrows, hrows.data(), hrows.size()));
+    TB_TRY(upload(ctx, pp.nptr, nptr.data(), nptr.size()));
+    TB_TRY(upload(ctx, pp.ngrp, ngrp.data(), ngrp.size()));
+    TB_TRY(dalloc(ctx, pp.flags, (size_t)G * best.nc));
+    TB_TRY(dalloc(ctx, pp.err, 1));
+    TB_CUDA(cudaMemsetAsync(pp.err, 0, sizeof(int32_t), ctx->stream));
+    // re-apply the chosen shared-memory size (setup ran for several candidates)
+    int per_sm = 0;
+    cheb_f32_persistent_setup(R, cheb_f32_persistent_smem(R, best.maxH, best.maxBlk, best.maxNG), &per_sm);
+    pp.R = R;
+    pp.G = G;
+    pp.nc = best.nc;
+    pp.B = best.B;
+    pp.maxH = best.maxH;
+    pp.maxBlk = best.maxBlk;
+    pp.maxNG = best.maxNG;
+    return TB_OK;
+}
+
 std::pair<cudaEvent_t, cudaEvent_t> next_events(tb_ctx *ctx)
 {
     if (ctx->ev_used == ctx->moment_events.size()) {
@@ -328,8 +537,10 @@ int density_eval(tb_ctx *ctx, bool have_shift)
     const int nslab = (m.n + B - 1) / B;
     for (int s = 0; s < nslab; s++) {
         const int c0 = s * B;
-        launch_slab_identity(st, w.T0, m.n, B, c0, p.precision);
-        ctx->launches++;
+        if (!w.persist) {
+            launch_slab_identity(st, w.T0, m.n, B, c0, p.precision);
+            ctx->launches++;
+        }
         if (p.precision == TB_PREC_FP64) {
             double *A = (double *)w.T0, *Bf = (double *)w.T1;
             for (int kout = 1; kout <= M; kout++) {
@@ -339,6 +550,18 @@ int density_eval(tb_ctx *ctx, bool have_shift)
             }
             ctx->spmm_launches += M;
             ctx->spmm_bytes += M * step_bytes(m, B, 8);
+        } else if (w.persist) {
+            TB_CUDA(cudaMemsetAsync(ctx->pp.flags, 0, sizeof(int32_t) * ctx->pp.G * ctx->pp.nc, st));
+            const int e = launch_cheb_f32_persistent(st, m, ctx->pp, w.K, B, c0, (float *)w.T0,
+                                                     (float *)w.T1, w.partial, ctx->pp.flags,
+                                                     ctx->pp.err);
+            if (e != (int)cudaSuccess)
+                return fail(ctx, TB_ERR_CUDA,
+                            std::string("cooperative launch: ") + cudaGetErrorString((cudaError_t)e));
+            launch_f32_finalize(st, m, w.partial, w.K, w.rowgroups, B, c0, w.d, M);
+            ctx->launches += 2;
+            ctx->spmm_launches += w.K;  // one launch carries all K slab steps
+            ctx->spmm_bytes += w.K * step_bytes(m, B, 4);
         } else {
             float *A = (float *)w.T0, *Bf = (float *)w.T1;
             for (int k = 0; k < w.K; k++) {
@@ -379,8 +602,15 @@ int density_eval(tb_ctx *ctx, bool have_shift)
 
 int read_state(tb_ctx *ctx, DevState &hs)
 {
+    int32_t perr = 0;
     TB_CUDA(cudaMemcpyAsync(&hs, ctx->w.state, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+    if (ctx->pp.err)
+        TB_CUDA(cudaMemcpyAsync(&perr, ctx->pp.err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
     TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (perr) {
+        cudaMemsetAsync(ctx->pp.err, 0, sizeof(int32_t), ctx->stream);
+        return fail(ctx, TB_ERR_CUDA, "persistent Chebyshev kernel: neighbour wait timed out");
+    }
     return TB_OK;
 }
 
@@ -491,6 +721,14 @@ void free_all(tb_ctx *ctx)
     dfree(ctx->sp.lcol);
     dfree(ctx->sp.lself);
     ctx->sp = StagePlan{};
+    dfree(ctx->pp.lcode);
+    dfree(ctx->pp.hptr);
+    dfree(ctx->pp.hrows);
+    dfree(ctx->pp.nptr);
+    dfree(ctx->pp.ngrp);
+    dfree(ctx->pp.flags);
+    dfree(ctx->pp.err);
+    ctx->pp = PersistPlan{};
     if (ctx->sp2_scratch) cudaFree(ctx->sp2_scratch);
     ctx->sp2_scratch = nullptr;
 }
@@ -540,7 +778,7 @@ int tb_params_init(tb_params *p)
     p->mu_tol = 1e-9;
     p->scc_tol = 1e-6;
     p->scc_max_iter = 100;
-    p->mix_history = 8;
+    p->mix_history = 12;
     p->mix_beta = 0.2;
     p->sp2_drop_tol = 1e-5;
     p->sp2_max_iter = 40;
@@ -702,6 +940,7 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
         }
     free_all(ctx);
     ctx->have_h = ctx->have_scc = false;
+    ctx->tuned[0] = ctx->tuned[1] = 0;
     DevMatrix &m = ctx->m;
     m.n = n;
     m.natoms = natoms;
@@ -716,6 +955,7 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
     TB_TRY(upload(ctx, m.radius, radius.data(), radius.size()));
     TB_TRY(dalloc(ctx, m.xdiag32, (size_t)n));
     TB_TRY(build_stage_plan(ctx, brow, bcol));
+    TB_TRY(build_persist_plan(ctx, brow, bcol));
     // quadrature capacity: host Gershgorin width of H0, 2x margin for shifts
     double mn = 1e300, mx = -1e300;
     for (int i = 0; i < n; i++) {

@@ -60,6 +60,18 @@ struct StagePlan {
     int32_t *lself = nullptr;     // nb: local index of block row I in its own group's list
 };
 
+// Task plan of the persistent FP32 kernel (see k_cheb_f32_persistent).
+struct PersistPlan {
+    int32_t R = 0, G = 0, nc = 0, B = 0, maxH = 0, maxBlk = 0, maxNG = 0;
+    int32_t *lcode = nullptr;  // nnzb: own row r (< R) or R + halo index
+    int32_t *hptr = nullptr;   // G+1
+    int32_t *hrows = nullptr;  // halo block rows per group
+    int32_t *nptr = nullptr;   // G+1
+    int32_t *ngrp = nullptr;   // neighbouring groups per group
+    int32_t *flags = nullptr;  // G * nc step counters
+    int32_t *err = nullptr;    // device wait-timeout flag
+};
+
 struct DevScc {
     int32_t natoms = 0;
     int64_t nnz = 0;
@@ -76,6 +88,7 @@ struct DevWork {
     int32_t M = 0, nq_cap = 0, B = 0, K = 0, rowgroups = 0;
     int32_t precision = -1;
     int32_t kernel = -1;
+    bool persist = false;       // FP32 form through k_cheb_f32_persistent
     double *shift = nullptr;   // n
     double *d = nullptr;       // (M+1) * n diagonal moments [k][i]
     double *mom = nullptr;     // M+1
@@ -106,13 +119,14 @@ struct tb_ctx {
     tb::DevScc s;
     tb::DevWork w;
     tb::StagePlan sp;
+    tb::PersistPlan pp;
     int64_t launches = 0;
     int64_t spmm_launches = 0;
     double spmm_bytes = 0.0;
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> moment_events;
     size_t ev_used = 0;
-    int autotuned_B[2] = {0, 0};
+    int tuned[2] = {0, 0};  // per precision: 0 untuned, -1 persistent, else slab width
     // SP2 device scratch (lazily sized)
     void *sp2_scratch = nullptr;
     size_t sp2_scratch_bytes = 0;
@@ -138,6 +152,11 @@ void launch_cheb_step_f32(cudaStream_t st, const DevMatrix &m, const float *Tin,
 int cheb_f32_rowgroups(int nb);
 size_t cheb_f32_staged_smem(int R, int maxU, int maxBlk);
 int cheb_f32_staged_configure(size_t smem);  // returns a cudaError_t
+size_t cheb_f32_persistent_smem(int R, int maxH, int maxBlk, int maxNG);
+int cheb_f32_persistent_setup(int R, size_t smem, int *ctas_per_sm);  // returns a cudaError_t
+int launch_cheb_f32_persistent(cudaStream_t st, const DevMatrix &m, const PersistPlan &pp, int K,
+                               int B, int c0, float *G0, float *G1, double *partial, int *flags,
+                               int *err);  // returns a cudaError_t
 int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const StagePlan &sp,
                                 const float *Tin, float *Tout, int B, int first,
                                 double *partial_k);

@@ -25,6 +25,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "tb_internal.h"
 
 namespace tb {
@@ -584,6 +586,289 @@ int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const Stage
                                                          Tout, B, first, partial_k, sp.maxU,
                                                          sp.maxBlk);
     return 1;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 Chebyshev recurrence, persistent form: one cooperative launch runs all
+// K steps of a slab.  CTA = one task (row group g of R block rows x one
+// 64-column chunk), resident for the whole launch; its own rows of T_k and
+// T_{k-1} stay in shared memory, so a step stages only the group's halo rows
+// (the referenced rows owned by other groups) from global memory.  A task
+// publishes its T_{k+1} rows to global buffer (k+1)%2 and then its step
+// count in flags[task] (release); before step k it waits until every
+// neighbouring task of the same chunk has published step k (acquire).  The
+// block pattern is symmetric, so that one wait also guarantees that no
+// neighbour still reads the buffer about to be overwritten.  Waits are
+// bounded: past kSpinLimit polls the kernel raises *err and every CTA leaves
+// at its next wait.  Co-residency of all tasks comes from the cooperative
+// launch, which the host only uses when the tasks fit the device.
+// ---------------------------------------------------------------------------
+constexpr int kPCols = 64;
+constexpr int kPWarps = 8;
+constexpr long long kSpinLimit = 1ll << 24;
+
+__device__ __forceinline__ int ld_acquire_gpu(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+template <int kRPW>  // block rows per warp kept in registers: R <= 8 kRPW
+__global__ void __launch_bounds__(32 * kPWarps, (kRPW <= 4 ? 3 : 2))
+    k_cheb_f32_persistent(int nb, int R, int nc, int K, int B, int c0, const int32_t *__restrict__ rowptr,
+                          const int32_t *__restrict__ lcode, const int32_t *__restrict__ hptr,
+                          const int32_t *__restrict__ hrows, const int32_t *__restrict__ nptr,
+                          const int32_t *__restrict__ ngrp, const float *__restrict__ x32,
+                          float *__restrict__ G0, float *__restrict__ G1, double *__restrict__ partial,
+                          int G, int *__restrict__ flags, int *__restrict__ err, int maxH, int maxBlk,
+                          int maxNG)
+{
+    extern __shared__ float4 psm4[];
+    const int rowf = 4 * kPCols;  // floats per staged block row
+    float *own0 = reinterpret_cast<float *>(psm4);
+    float *own1 = own0 + R * rowf;
+    float *halo = own1 + R * rowf;  // also the dot-product reduction buffer
+    const int halo_f = max(maxH * rowf, kPWarps * kPCols * 4);
+    float *sX = halo + halo_f;
+    int *sL = reinterpret_cast<int *>(sX + maxBlk * 16);
+    int *sR = sL + maxBlk;
+    int *sH = sR + R + 1;
+    int *sN = sH + max(maxH, 1);
+    const int task = blockIdx.x, g = task / nc, c = task % nc, col0 = c * kPCols;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, cl = 2 * lane;
+    const int I0 = g * R, nr = min(R, nb - I0);
+    const int tb0 = rowptr[I0], nbk = rowptr[I0 + nr] - tb0;
+    const int h0 = hptr[g], nh = hptr[g + 1] - h0;
+    const int n0 = nptr[g], nn = nptr[g + 1] - n0;
+    for (int i = tid; i < nbk; i += blockDim.x) sL[i] = lcode[tb0 + i];
+    for (int i = tid; i <= nr; i += blockDim.x) sR[i] = rowptr[I0 + i] - tb0;
+    for (int i = tid; i < nh; i += blockDim.x) sH[i] = hrows[h0 + i];
+    for (int i = tid; i < nn; i += blockDim.x) sN[i] = ngrp[n0 + i];
+    for (int idx = tid; idx < nbk * 4; idx += blockDim.x)
+        cp_async16(sX + idx * 4, x32 + (int64_t)tb0 * 16 + idx * 4);
+    // own rows of T_0: the identity columns c0 + col0 .. c0 + col0 + 63
+    for (int e = tid; e < nr * rowf; e += blockDim.x) {
+        const int r = e / rowf, m = (e / kPCols) & 3, j = e % kPCols;
+        own0[e] = (4 * (I0 + r) + m == c0 + col0 + j) ? 1.f : 0.f;
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const volatile int *verr = err;
+    __shared__ int s_stop;
+    for (int k = 0; k < K; k++) {
+        float *cur = (k & 1) ? own1 : own0;
+        float *prev = (k & 1) ? own0 : own1;
+        const float *Gk = (k & 1) ? G1 : G0;
+        float *Gn = (k & 1) ? G0 : G1;
+        // ---- 1. contributions of the own rows (in shared memory already),
+        // computed before waiting so the wait overlaps with work ----
+        float acc[kRPW][4][2];
+#pragma unroll
+        for (int j = 0; j < kRPW; j++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc[j][q][0] = acc[j][q][1] = 0.f;
+#pragma unroll
+        for (int j = 0; j < kRPW; j++) {
+            const int r = w + j * kPWarps;
+            if (r >= nr) break;
+            for (int t = sR[r]; t < sR[r + 1]; t++) {
+                const int code = sL[t];
+                if (code >= R) continue;
+                const float *tv = cur + code * rowf + cl;
+                const float4 *xb = reinterpret_cast<const float4 *>(sX + t * 16);
+                float2 v[4];
+#pragma unroll
+                for (int m = 0; m < 4; m++) v[m] = *reinterpret_cast<const float2 *>(tv + m * kPCols);
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float4 xr = xb[q];
+                    const float xm[4] = {xr.x, xr.y, xr.z, xr.w};
+#pragma unroll
+                    for (int m = 0; m < 4; m++) {
+                        acc[j][q][0] = fmaf(xm[m], v[m].x, acc[j][q][0]);
+                        acc[j][q][1] = fmaf(xm[m], v[m].y, acc[j][q][1]);
+                    }
+                }
+            }
+        }
+        // ---- 2. wait for the neighbours' step k: warp 0, one lane per
+        // neighbour; the stop decision is broadcast through shared memory so
+        // the CTA leaves as one ----
+        if (w == 0) {
+            bool give_up = false;
+            if (k > 0) {
+                for (int i0 = 0; i0 < nn; i0 += 32) {
+                    const int i = i0 + lane;
+                    const int *f = i < nn ? flags + sN[i] * nc + c : nullptr;
+                    long long spins = 0;
+                    bool ready = (f == nullptr);
+                    while (!__all_sync(0xffffffffu, ready)) {
+                        if (!ready) ready = ld_acquire_gpu(f) >= k;
+                        if (__any_sync(0xffffffffu, *verr != 0)) {
+                            give_up = true;
+                            break;
+                        }
+                        if (++spins > kSpinLimit) {
+                            if (lane == 0) atomicExch(err, 1);
+                            give_up = true;
+                            break;
+                        }
+                        __nanosleep(20);
+                    }
+                    if (give_up) break;
+                }
+                __threadfence();
+            }
+            if (lane == 0) s_stop = give_up ? 1 : *verr;
+        }
+        __syncthreads();
+        if (s_stop) return;  // no copies are in flight here
+        // ---- 3. halo rows of T_k ----
+        if (k == 0) {
+            for (int e = tid; e < nh * rowf; e += blockDim.x) {
+                const int h = e / rowf, m = (e / kPCols) & 3, j = e % kPCols;
+                halo[e] = (4 * sH[h] + m == c0 + col0 + j) ? 1.f : 0.f;
+            }
+        } else {
+            for (int idx = tid; idx < nh * 64; idx += blockDim.x) {
+                const int h = idx >> 6, m = (idx >> 4) & 3, sg = idx & 15;
+                cp_async16(halo + (h * 4 + m) * kPCols + sg * 4,
+                           Gk + (int64_t)(4 * sH[h] + m) * B + col0 + sg * 4);
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        // ---- 4. halo contributions, T_{k+1} for the own rows, dot products ----
+        double see[2] = {0.0, 0.0}, seo[2] = {0.0, 0.0};
+#pragma unroll
+        for (int j = 0; j < kRPW; j++) {
+            const int r = w + j * kPWarps;
+            if (r >= nr) break;
+            for (int t = sR[r]; t < sR[r + 1]; t++) {
+                const int code = sL[t];
+                if (code < R) continue;
+                const float *tv = halo + (code - R) * rowf + cl;
+                const float4 *xb = reinterpret_cast<const float4 *>(sX + t * 16);
+                float2 v[4];
+#pragma unroll
+                for (int m = 0; m < 4; m++) v[m] = *reinterpret_cast<const float2 *>(tv + m * kPCols);
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float4 xr = xb[q];
+                    const float xm[4] = {xr.x, xr.y, xr.z, xr.w};
+#pragma unroll
+                    for (int m = 0; m < 4; m++) {
+                        acc[j][q][0] = fmaf(xm[m], v[m].x, acc[j][q][0]);
+                        acc[j][q][1] = fmaf(xm[m], v[m].y, acc[j][q][1]);
+                    }
+                }
+            }
+            float ee[2] = {0.f, 0.f}, eo[2] = {0.f, 0.f};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float2 ov = *reinterpret_cast<const float2 *>(cur + r * rowf + q * kPCols + cl);
+                float2 *pv = reinterpret_cast<float2 *>(prev + r * rowf + q * kPCols + cl);
+                float2 o;
+                if (k == 0) {
+                    o = make_float2(acc[j][q][0], acc[j][q][1]);
+                } else {
+                    const float2 p = *pv;
+                    o.x = 2.f * acc[j][q][0] - p.x;
+                    o.y = 2.f * acc[j][q][1] - p.y;
+                }
+                *pv = o;
+                *reinterpret_cast<float2 *>(Gn + (int64_t)(4 * (I0 + r) + q) * B + col0 + cl) = o;
+                ee[0] = fmaf(ov.x, ov.x, ee[0]);
+                ee[1] = fmaf(ov.y, ov.y, ee[1]);
+                eo[0] = fmaf(ov.x, o.x, eo[0]);
+                eo[1] = fmaf(ov.y, o.y, eo[1]);
+            }
+            see[0] += (double)ee[0];
+            see[1] += (double)ee[1];
+            seo[0] += (double)eo[0];
+            seo[1] += (double)eo[1];
+        }
+        // ---- publish T_{k+1} ----
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) st_release_gpu(flags + task, k + 1);
+        // ---- per-column partial sums (the halo buffer is free now) ----
+        double *red = reinterpret_cast<double *>(halo);
+        red[(w * kPCols + cl) * 2 + 0] = see[0];
+        red[(w * kPCols + cl) * 2 + 1] = seo[0];
+        red[(w * kPCols + cl + 1) * 2 + 0] = see[1];
+        red[(w * kPCols + cl + 1) * 2 + 1] = seo[1];
+        __syncthreads();
+        if (tid < 2 * kPCols) {
+            const int j = tid >> 1, which = tid & 1;
+            double sacc = 0.0;
+#pragma unroll
+            for (int q = 0; q < kPWarps; q++) sacc += red[(q * kPCols + j) * 2 + which];
+            partial[(((int64_t)k * G + g) * B + col0 + j) * 2 + which] = sacc;
+        }
+        __syncthreads();
+    }
+}
+
+size_t cheb_f32_persistent_smem(int R, int maxH, int maxBlk, int maxNG)
+{
+    const size_t rowf = 4 * kPCols;
+    const size_t halo_f = std::max((size_t)maxH * rowf, (size_t)kPWarps * kPCols * 4);
+    return (2 * (size_t)R * rowf + halo_f + (size_t)maxBlk * 16) * sizeof(float) +
+           ((size_t)maxBlk + R + 1 + std::max(maxH, 1) + maxNG) * sizeof(int);
+}
+
+static int persistent_rpw(int R) { return (R + kPWarps - 1) / kPWarps; }
+
+template <int kRPW>
+static int persistent_setup_t(size_t smem, int *ctas_per_sm)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_cheb_f32_persistent<kRPW>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_cheb_f32_persistent<kRPW>,
+                                                              32 * kPWarps, smem);
+}
+
+int cheb_f32_persistent_setup(int R, size_t smem, int *ctas_per_sm)
+{
+    switch (persistent_rpw(R)) {
+    case 2: return persistent_setup_t<2>(smem, ctas_per_sm);
+    case 3: return persistent_setup_t<3>(smem, ctas_per_sm);
+    case 4: return persistent_setup_t<4>(smem, ctas_per_sm);
+    case 6: return persistent_setup_t<6>(smem, ctas_per_sm);
+    case 8: return persistent_setup_t<8>(smem, ctas_per_sm);
+    default: return (int)cudaErrorInvalidValue;
+    }
+}
+
+int launch_cheb_f32_persistent(cudaStream_t st, const DevMatrix &m, const PersistPlan &pp, int K,
+                               int B, int c0, float *G0, float *G1, double *partial, int *flags,
+                               int *err)
+{
+    const size_t smem = cheb_f32_persistent_smem(pp.R, pp.maxH, pp.maxBlk, pp.maxNG);
+    int nb = m.nb, R = pp.R, nc = pp.nc, G = pp.G, maxH = pp.maxH, maxBlk = pp.maxBlk,
+        maxNG = pp.maxNG;
+    const int32_t *rowptr = m.rowptr, *lcode = pp.lcode, *hptr = pp.hptr, *hrows = pp.hrows,
+                  *nptr = pp.nptr, *ngrp = pp.ngrp;
+    const float *x32 = m.x32;
+    void *args[] = {&nb, &R, &nc, &K, &B, &c0, &rowptr, &lcode, &hptr, &hrows, &nptr, &ngrp,
+                    &x32, &G0, &G1, &partial, &G, &flags, &err, &maxH, &maxBlk, &maxNG};
+    const void *fn = nullptr;
+    switch (persistent_rpw(pp.R)) {
+    case 2: fn = (const void *)k_cheb_f32_persistent<2>; break;
+    case 3: fn = (const void *)k_cheb_f32_persistent<3>; break;
+    case 4: fn = (const void *)k_cheb_f32_persistent<4>; break;
+    case 6: fn = (const void *)k_cheb_f32_persistent<6>; break;
+    case 8: fn = (const void *)k_cheb_f32_persistent<8>; break;
+    default: return (int)cudaErrorInvalidValue;
+    }
+    return (int)cudaLaunchCooperativeKernel(fn, dim3(G * nc), dim3(32 * kPWarps), args, smem, st);
 }
 
 // Sum the per-rowgroup partials of a slab and turn them into moments:
