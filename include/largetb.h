@@ -192,6 +192,38 @@ int tb_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep
 int tb_kpm_dos(tb_ctx *ctx, int32_t n_moments, int32_t n_random, uint64_t seed, int32_t npts,
                double *moments, double *energies, double *dos, tb_report *rep);
 
+/* ------------------------------------------------------------------------ */
+/* Batches: many structures of uneven size in one solve                      */
+/* ------------------------------------------------------------------------ */
+/* The reference solves one structure per run (main, withSP2_deltaH.cpp:
+ * 1742-1849).  A batch solves `count` independent structures together: each
+ * structure keeps its own Gershgorin scaling, chemical potential, Anderson
+ * history and convergence test on the device, while every Chebyshev step of
+ * all still-unconverged structures runs as one launch (FP32 recurrence, FP64
+ * moments; the precision field is ignored).  M, kT, kernel, the SCC
+ * tolerance, mixer and iteration cap come from p; n_electrons <= 0 takes
+ * sum(q0) per structure. */
+typedef struct tb_batch tb_batch;
+
+int tb_batch_create(const tb_params *p, int32_t count, tb_batch **out);
+int tb_batch_destroy(tb_batch *b);
+
+/* Structure `index`: its Hamiltonian (the tb_set_hamiltonian input, orbitals
+ * 4 per atom, contiguous), Gamma and neutral charges (the tb_set_scc input). */
+int tb_batch_set(tb_batch *b, int32_t index, int32_t n, const int32_t *rowptr,
+                 const int32_t *colidx, const double *vals, int32_t natoms,
+                 const int32_t *g_rowptr, const int32_t *g_colidx, const double *g_vals,
+                 const double *q0);
+
+/* SCC solve of every structure.  q_init (may be NULL) and q are the
+ * structures' atoms concatenated in index order; iters, e_band and mu have
+ * `count` entries.  Returns TB_ERR_NOT_CONVERGED if any structure reached
+ * scc_max_iter (all outputs still written). */
+int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *iters,
+                       double *e_band, double *mu, tb_report *rep);
+
+const char *tb_batch_last_error(const tb_batch *b);
+
 /* Message of the last failure on ctx (never NULL). */
 const char *tb_last_error(const tb_ctx *ctx);
 const char *tb_status_string(int status);

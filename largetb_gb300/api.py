@@ -149,6 +149,13 @@ def load(build_if_missing: bool = True):
                                  C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.tb_model_export.argtypes = [_vp] + [_vp] * 10
     L.tb_model_destroy.argtypes = [_vp]
+    L.tb_batch_create.argtypes = [C.POINTER(TbParams), C.c_int32, C.POINTER(_vp)]
+    L.tb_batch_destroy.argtypes = [_vp]
+    L.tb_batch_set.argtypes = [_vp, C.c_int32, C.c_int32, _i32p, _i32p, _f64p, C.c_int32, _i32p,
+                               _i32p, _f64p, _f64p]
+    L.tb_batch_scc_solve.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(TbReport)]
+    L.tb_batch_last_error.argtypes = [_vp]
+    L.tb_batch_last_error.restype = C.c_char_p
     _lib = L
     return L
 
@@ -361,3 +368,59 @@ class Context:
         self._check(self._L.tb_kpm_dos(self._h, n_moments, n_random, seed, npts, _ptr(mom), _ptr(e),
                                        _ptr(dos), C.byref(rep)))
         return dict(moments=mom, energies=e, dos=dos, report=rep.as_dict())
+
+
+class Batch:
+    """Many structures solved together (tb_batch_*): per-structure scaling,
+    mu, Anderson state and convergence on the device, one launch per
+    Chebyshev step for all unconverged structures."""
+
+    def __init__(self, models, p: TbParams | None = None, **kw):
+        self._L = load()
+        self.p = p if p is not None else params(**kw)
+        h = _vp()
+        rc = self._L.tb_batch_create(C.byref(self.p), len(models), C.byref(h))
+        if rc:
+            raise TbError(rc, self._L.tb_status_string(rc).decode())
+        self._h = h
+        self.natoms = [m.natoms for m in models]
+        for i, m in enumerate(models):
+            self._check(self._L.tb_batch_set(self._h, i, m.n, m.rowptr, m.colidx, m.vals, m.natoms,
+                                             m.g_rowptr, m.g_colidx, m.g_vals, m.q0))
+
+    def _check(self, rc, allow=()):
+        if rc != TB_OK and rc not in allow:
+            raise TbError(rc, self._L.tb_batch_last_error(self._h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.tb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def scc_solve(self, q_init=None, raise_on_cap=True):
+        S = len(self.natoms)
+        q = np.zeros(sum(self.natoms))
+        it = np.zeros(S, np.int32)
+        eb = np.zeros(S)
+        mu = np.zeros(S)
+        rep = TbReport()
+        qi = None if q_init is None else np.ascontiguousarray(q_init, np.float64)
+        rc = self._check(self._L.tb_batch_scc_solve(self._h, _ptr(qi), _ptr(q), _ptr(it), _ptr(eb),
+                                                    _ptr(mu), C.byref(rep)),
+                         allow=() if raise_on_cap else (TB_ERR_NOT_CONVERGED,))
+        offs = np.cumsum([0] + self.natoms)
+        return dict(status=rc, q=[q[offs[i]:offs[i + 1]] for i in range(S)], iters=it, e_band=eb,
+                    mu=mu, report=rep.as_dict())

@@ -735,6 +735,141 @@ void free_all(tb_ctx *ctx)
 
 }  // namespace
 
+namespace tb {
+
+// Validation and conversion of a PETSc-style CSR (4 orbitals per atom) to
+// symmetrised 4x4 BSR on the host: the pattern of H + H^T with every diagonal
+// block present, values (H + H^T)/2 (runKPM, withSP2_deltaH.cpp:1536-1538),
+// Gershgorin centres and radii.
+int host_csr_to_bsr(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                    const int32_t *orb2atom, int32_t natoms, HostBsr &hb, std::string &err)
+{
+    auto bad = [&](int code, const char *msg) {
+        err = msg;
+        return code;
+    };
+    if (n <= 0 || natoms <= 0 || !rowptr || !colidx || !vals || !orb2atom)
+        return bad(TB_ERR_INVALID_ARG, "null array or non-positive size");
+    if ((int64_t)natoms * 4 != n)
+        return bad(TB_ERR_STRUCTURE, "n must be 4 * natoms (sp3: 4 orbitals per atom)");
+    for (int i = 0; i < n; i++)
+        if (orb2atom[i] != i / 4)
+            return bad(TB_ERR_STRUCTURE,
+                       "orb2atom must map orbitals 4a..4a+3 to atom a (contiguous sp3 blocks)");
+    if (rowptr[0] != 0) return bad(TB_ERR_STRUCTURE, "rowptr[0] != 0");
+    for (int i = 0; i < n; i++) {
+        if (rowptr[i + 1] < rowptr[i]) return bad(TB_ERR_STRUCTURE, "rowptr not monotone");
+        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+            if (colidx[k] < 0 || colidx[k] >= n) return bad(TB_ERR_STRUCTURE, "column index out of range");
+            if (k > rowptr[i] && colidx[k] <= colidx[k - 1])
+                return bad(TB_ERR_STRUCTURE, "column indices not strictly increasing");
+            if (!std::isfinite(vals[k])) return bad(TB_ERR_NONFINITE, "NaN/Inf in Hamiltonian");
+        }
+    }
+    const int nb = natoms;
+    std::vector<std::vector<int32_t>> pat(nb);
+    for (int I = 0; I < nb; I++) pat[I].push_back(I);
+    for (int i = 0; i < n; i++)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+            const int I = i / 4, J = colidx[k] / 4;
+            pat[I].push_back(J);
+            pat[J].push_back(I);
+        }
+    hb.brow.assign(nb + 1, 0);
+    for (int I = 0; I < nb; I++) {
+        auto &v = pat[I];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        hb.brow[I + 1] = hb.brow[I] + (int32_t)v.size();
+    }
+    const int64_t nnzb = hb.brow[nb];
+    hb.bcol.assign(nnzb, 0);
+    hb.blkrow.assign(nnzb, 0);
+    hb.diagblk.assign(nb, 0);
+    for (int I = 0; I < nb; I++)
+        for (size_t t = 0; t < pat[I].size(); t++) {
+            hb.bcol[hb.brow[I] + t] = pat[I][t];
+            hb.blkrow[hb.brow[I] + t] = I;
+            if (pat[I][t] == I) hb.diagblk[I] = hb.brow[I] + (int32_t)t;
+        }
+    pat.clear();
+    auto find_blk = [&](int I, int J) -> int64_t {
+        const int32_t *b = hb.bcol.data() + hb.brow[I], *e = hb.bcol.data() + hb.brow[I + 1];
+        return (int64_t)(std::lower_bound(b, e, J) - hb.bcol.data());
+    };
+    hb.blk.assign((size_t)nnzb * 16, 0.0);
+    hb.asym = 0.0;
+    for (int i = 0; i < n; i++)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+            const int j = colidx[k];
+            const double v = vals[k];
+            const int64_t t1 = find_blk(i / 4, j / 4), t2 = find_blk(j / 4, i / 4);
+            hb.blk[t1 * 16 + (i % 4) * 4 + (j % 4)] += 0.5 * v;
+            hb.blk[t2 * 16 + (j % 4) * 4 + (i % 4)] += 0.5 * v;
+            const int32_t *b = colidx + rowptr[j], *e = colidx + rowptr[j + 1];
+            const int32_t *it = std::lower_bound(b, e, i);
+            const double vt = (it != e && *it == i) ? vals[rowptr[j] + (it - b)] : 0.0;
+            hb.asym = std::max(hb.asym, std::fabs(v - vt));
+        }
+    hb.h0diag.assign(n, 0.0);
+    hb.radius.assign(n, 0.0);
+    hb.lmin = 1e300;
+    hb.lmax = -1e300;
+    for (int I = 0; I < nb; I++)
+        for (int r = 0; r < 4; r++) {
+            double rad = 0.0, dg = 0.0;
+            for (int t = hb.brow[I]; t < hb.brow[I + 1]; t++)
+                for (int c = 0; c < 4; c++) {
+                    const double v = hb.blk[(size_t)t * 16 + r * 4 + c];
+                    if (hb.bcol[t] == I && c == r)
+                        dg = v;
+                    else
+                        rad += std::fabs(v);
+                }
+            hb.h0diag[4 * I + r] = dg;
+            hb.radius[4 * I + r] = rad;
+            hb.lmin = std::min(hb.lmin, dg - rad);
+            hb.lmax = std::max(hb.lmax, dg + rad);
+        }
+    return TB_OK;
+}
+
+int host_check_gamma(int32_t natoms, const int32_t *g_rowptr, const int32_t *g_colidx,
+                     const double *g_vals, const double *q0, std::string &err)
+{
+    if (!g_rowptr || !g_colidx || !g_vals || !q0) {
+        err = "null Gamma or q0 array";
+        return TB_ERR_INVALID_ARG;
+    }
+    if (g_rowptr[0] != 0) {
+        err = "Gamma rowptr[0] != 0";
+        return TB_ERR_STRUCTURE;
+    }
+    for (int a = 0; a < natoms; a++) {
+        if (g_rowptr[a + 1] < g_rowptr[a]) {
+            err = "Gamma rowptr not monotone";
+            return TB_ERR_STRUCTURE;
+        }
+        for (int k = g_rowptr[a]; k < g_rowptr[a + 1]; k++) {
+            if (g_colidx[k] < 0 || g_colidx[k] >= natoms) {
+                err = "Gamma column out of range";
+                return TB_ERR_STRUCTURE;
+            }
+            if (!std::isfinite(g_vals[k])) {
+                err = "NaN/Inf in Gamma";
+                return TB_ERR_NONFINITE;
+            }
+        }
+        if (!std::isfinite(q0[a])) {
+            err = "NaN/Inf in q0";
+            return TB_ERR_NONFINITE;
+        }
+    }
+    return TB_OK;
+}
+
+}  // namespace tb
+
 // ===========================================================================
 // C-ABI
 // ===========================================================================
@@ -856,116 +991,32 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
                        const double *vals, const int32_t *orb2atom, int32_t natoms)
 {
     if (!ctx) return TB_ERR_INVALID_ARG;
-    if (n <= 0 || natoms <= 0 || !rowptr || !colidx || !vals || !orb2atom)
-        return fail(ctx, TB_ERR_INVALID_ARG, "null array or non-positive size");
-    if ((int64_t)natoms * 4 != n)
-        return fail(ctx, TB_ERR_STRUCTURE, "n must be 4 * natoms (sp3: 4 orbitals per atom)");
-    for (int i = 0; i < n; i++)
-        if (orb2atom[i] != i / 4)
-            return fail(ctx, TB_ERR_STRUCTURE,
-                        "orb2atom must map orbitals 4a..4a+3 to atom a (contiguous sp3 blocks)");
-    if (rowptr[0] != 0) return fail(ctx, TB_ERR_STRUCTURE, "rowptr[0] != 0");
-    for (int i = 0; i < n; i++) {
-        if (rowptr[i + 1] < rowptr[i]) return fail(ctx, TB_ERR_STRUCTURE, "rowptr not monotone");
-        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
-            if (colidx[k] < 0 || colidx[k] >= n)
-                return fail(ctx, TB_ERR_STRUCTURE, "column index out of range");
-            if (k > rowptr[i] && colidx[k] <= colidx[k - 1])
-                return fail(ctx, TB_ERR_STRUCTURE, "column indices not strictly increasing");
-            if (!std::isfinite(vals[k])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in Hamiltonian");
-        }
-    }
+    HostBsr hb;
+    const int vrc = host_csr_to_bsr(n, rowptr, colidx, vals, orb2atom, natoms, hb, ctx->err);
+    if (vrc) return vrc;
     TB_TRY(set_device(ctx));
-    const int nb = natoms;
-    // block pattern of H + H^T, diagonal always present
-    std::vector<std::vector<int32_t>> pat(nb);
-    for (int I = 0; I < nb; I++) pat[I].push_back(I);
-    for (int i = 0; i < n; i++)
-        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
-            const int I = i / 4, J = colidx[k] / 4;
-            pat[I].push_back(J);
-            pat[J].push_back(I);
-        }
-    std::vector<int32_t> brow(nb + 1, 0);
-    for (int I = 0; I < nb; I++) {
-        auto &v = pat[I];
-        std::sort(v.begin(), v.end());
-        v.erase(std::unique(v.begin(), v.end()), v.end());
-        brow[I + 1] = brow[I] + (int32_t)v.size();
-    }
-    const int64_t nnzb = brow[nb];
-    std::vector<int32_t> bcol(nnzb), blkrow(nnzb), diagblk(nb);
-    for (int I = 0; I < nb; I++)
-        for (size_t t = 0; t < pat[I].size(); t++) {
-            bcol[brow[I] + t] = pat[I][t];
-            blkrow[brow[I] + t] = I;
-            if (pat[I][t] == I) diagblk[I] = brow[I] + (int32_t)t;
-        }
-    pat.clear();
-    pat.shrink_to_fit();
-    auto find_blk = [&](int I, int J) -> int64_t {
-        const int32_t *b = bcol.data() + brow[I], *e = bcol.data() + brow[I + 1];
-        const int32_t *it = std::lower_bound(b, e, J);
-        return (int64_t)(it - bcol.data());
-    };
-    // (H + H^T)/2 as runKPM forms it (withSP2_deltaH.cpp:1536-1538)
-    std::vector<double> blk((size_t)nnzb * 16, 0.0);
-    double asym = 0.0;
-    for (int i = 0; i < n; i++)
-        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
-            const int j = colidx[k];
-            const double v = vals[k];
-            const int64_t t1 = find_blk(i / 4, j / 4), t2 = find_blk(j / 4, i / 4);
-            blk[t1 * 16 + (i % 4) * 4 + (j % 4)] += 0.5 * v;
-            blk[t2 * 16 + (j % 4) * 4 + (i % 4)] += 0.5 * v;
-            const int32_t *b = colidx + rowptr[j], *e = colidx + rowptr[j + 1];
-            const int32_t *it = std::lower_bound(b, e, i);
-            const double vt = (it != e && *it == i) ? vals[rowptr[j] + (it - b)] : 0.0;
-            asym = std::max(asym, std::fabs(v - vt));
-        }
-    std::vector<double> h0diag(n), radius(n);
-    for (int I = 0; I < nb; I++)
-        for (int r = 0; r < 4; r++) {
-            double rad = 0.0, dg = 0.0;
-            for (int t = brow[I]; t < brow[I + 1]; t++)
-                for (int c = 0; c < 4; c++) {
-                    const double v = blk[(size_t)t * 16 + r * 4 + c];
-                    if (bcol[t] == I && c == r)
-                        dg = v;
-                    else
-                        rad += std::fabs(v);
-                }
-            h0diag[4 * I + r] = dg;
-            radius[4 * I + r] = rad;
-        }
     free_all(ctx);
     ctx->have_h = ctx->have_scc = false;
     ctx->tuned[0] = ctx->tuned[1] = 0;
     DevMatrix &m = ctx->m;
     m.n = n;
     m.natoms = natoms;
-    m.nb = nb;
-    m.nnzb = nnzb;
-    TB_TRY(upload(ctx, m.rowptr, brow.data(), brow.size()));
-    TB_TRY(upload(ctx, m.colidx, bcol.data(), bcol.size()));
-    TB_TRY(upload(ctx, m.blkrow, blkrow.data(), blkrow.size()));
-    TB_TRY(upload(ctx, m.diagblk, diagblk.data(), diagblk.size()));
-    TB_TRY(upload(ctx, m.h0, blk.data(), blk.size()));
-    TB_TRY(upload(ctx, m.h0diag, h0diag.data(), h0diag.size()));
-    TB_TRY(upload(ctx, m.radius, radius.data(), radius.size()));
+    m.nb = natoms;
+    m.nnzb = (int64_t)hb.bcol.size();
+    TB_TRY(upload(ctx, m.rowptr, hb.brow.data(), hb.brow.size()));
+    TB_TRY(upload(ctx, m.colidx, hb.bcol.data(), hb.bcol.size()));
+    TB_TRY(upload(ctx, m.blkrow, hb.blkrow.data(), hb.blkrow.size()));
+    TB_TRY(upload(ctx, m.diagblk, hb.diagblk.data(), hb.diagblk.size()));
+    TB_TRY(upload(ctx, m.h0, hb.blk.data(), hb.blk.size()));
+    TB_TRY(upload(ctx, m.h0diag, hb.h0diag.data(), hb.h0diag.size()));
+    TB_TRY(upload(ctx, m.radius, hb.radius.data(), hb.radius.size()));
     TB_TRY(dalloc(ctx, m.xdiag32, (size_t)n));
-    TB_TRY(build_stage_plan(ctx, brow, bcol));
-    TB_TRY(build_persist_plan(ctx, brow, bcol));
-    // quadrature capacity: host Gershgorin width of H0, 2x margin for shifts
-    double mn = 1e300, mx = -1e300;
-    for (int i = 0; i < n; i++) {
-        mn = std::min(mn, h0diag[i] - radius[i]);
-        mx = std::max(mx, h0diag[i] + radius[i]);
-    }
-    ctx->h0_lmin = mn;
-    ctx->h0_lmax = mx;
+    TB_TRY(build_stage_plan(ctx, hb.brow, hb.bcol));
+    TB_TRY(build_persist_plan(ctx, hb.brow, hb.bcol));
+    ctx->h0_lmin = hb.lmin;
+    ctx->h0_lmax = hb.lmax;
     TB_CUDA(cudaStreamSynchronize(ctx->stream));
-    ctx->asym_max = asym;
+    ctx->asym_max = hb.asym;
     ctx->have_h = true;
     return TB_OK;
 }
@@ -975,17 +1026,10 @@ int tb_set_scc(tb_ctx *ctx, int32_t natoms, const int32_t *g_rowptr, const int32
 {
     if (!ctx) return TB_ERR_INVALID_ARG;
     if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "tb_set_hamiltonian must come first");
-    if (natoms != ctx->m.natoms || !g_rowptr || !g_colidx || !g_vals || !q0)
-        return fail(ctx, TB_ERR_INVALID_ARG, "natoms mismatch or null array");
-    if (g_rowptr[0] != 0) return fail(ctx, TB_ERR_STRUCTURE, "Gamma rowptr[0] != 0");
-    for (int a = 0; a < natoms; a++) {
-        if (g_rowptr[a + 1] < g_rowptr[a]) return fail(ctx, TB_ERR_STRUCTURE, "Gamma rowptr not monotone");
-        for (int k = g_rowptr[a]; k < g_rowptr[a + 1]; k++) {
-            if (g_colidx[k] < 0 || g_colidx[k] >= natoms)
-                return fail(ctx, TB_ERR_STRUCTURE, "Gamma column out of range");
-            if (!std::isfinite(g_vals[k])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in Gamma");
-        }
-        if (!std::isfinite(q0[a])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in q0");
+    if (natoms != ctx->m.natoms) return fail(ctx, TB_ERR_INVALID_ARG, "natoms mismatch");
+    {
+        const int grc = host_check_gamma(natoms, g_rowptr, g_colidx, g_vals, q0, ctx->err);
+        if (grc) return grc;
     }
     TB_TRY(set_device(ctx));
     DevScc &s = ctx->s;

@@ -175,6 +175,17 @@ void launch_charges(cudaStream_t st, const double *d, const double *c, const dou
 void launch_scc_update(cudaStream_t st, DevScc &s, const double *qout, double beta, int history,
                        double tol, double *shift, DevState *state);
 
+// ---- tb_api.cpp: host-side conversion shared by the context and the batch ----
+struct HostBsr {
+    std::vector<int32_t> brow, bcol, blkrow, diagblk;
+    std::vector<double> blk, h0diag, radius;
+    double asym = 0.0, lmin = 0.0, lmax = 0.0;
+};
+int host_csr_to_bsr(int32_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                    const int32_t *orb2atom, int32_t natoms, HostBsr &hb, std::string &err);
+int host_check_gamma(int32_t natoms, const int32_t *g_rowptr, const int32_t *g_colidx,
+                     const double *g_vals, const double *q0, std::string &err);
+
 // ---- tb_sp2.cu ----------------------------------------------------------
 // SP2 purification of the context's H; branches_out (optional) receives the
 // applied branch sequence (-1: X^2, +1: 2X - X^2).

@@ -1,0 +1,56 @@
+"""Batched SCC (tb_batch_*) against the oracle's SCC of each structure.
+
+Structures of different sizes share every Chebyshev launch but keep their own
+scaling, mu, Anderson state and convergence test; each must land where the
+oracle's own loop lands (FP32 recurrence: charges within 1e-6 e, iteration
+count within 1)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CASES = [((1, 1, 2), 0.05, 11), ((2, 1, 1), 0.08, 12), ((1, 2, 2), 0.03, 13)]
+
+
+def test_batch_matches_oracle(gpu):
+    models = [gpu.model_cristobalite(*c, sigma_ang=s, seed=sd) for c, s, sd in CASES]
+    M = 150
+    with gpu.Batch(models, M=M) as b:
+        r = b.scc_solve()
+    for i, (c, s, sd) in enumerate(CASES):
+        o = O.cristobalite(*c, sigma_ang=s, seed=sd)
+        ref = O.scc(o, O.kpe_params(M=M, kT=0.01, n_elec=o.n_elec), tol=1e-6, max_iter=100,
+                    beta=0.2, history=12)
+        assert ref["status"] == 0
+        assert abs(int(r["iters"][i]) - ref["iters"]) <= 1, (i, r["iters"][i], ref["iters"])
+        assert np.abs(r["q"][i] - ref["q"]).max() < 1e-6
+        assert abs(r["e_band"][i] - ref["e_band"]) / o.natoms < 1e-7
+
+
+def test_batch_agrees_with_single_structure_path(gpu):
+    models = [gpu.model_cristobalite(*c, sigma_ang=s, seed=sd) for c, s, sd in CASES]
+    with gpu.Batch(models, M=120) as b:
+        r = b.scc_solve()
+    for i, m in enumerate(models):
+        with gpu.Context(M=120, precision=gpu.PREC_FP32) as c:
+            c.set_model(m)
+            s = c.scc_solve()
+        assert abs(int(r["iters"][i]) - s["iters"]) <= 1
+        assert np.abs(r["q"][i] - s["q"]).max() < 1e-6
+
+
+def test_batch_unset_structure_is_reported(gpu):
+    m = gpu.model_cristobalite(1, 1, 1, sigma_ang=0.05, seed=1)
+    b = gpu.Batch([m], M=50)
+    b.close()
+    import ctypes as C
+    L = gpu.load()
+    h = C.c_void_p()
+    p = gpu.params(M=50)
+    assert L.tb_batch_create(C.byref(p), 2, C.byref(h)) == 0
+    rep = gpu.TbReport()
+    rc = L.tb_batch_scc_solve(h, None, None, None, None, None, C.byref(rep))
+    assert rc == gpu.api.TB_ERR_NOT_READY
+    L.tb_batch_destroy(h)
