@@ -148,6 +148,17 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
 int tb_set_scc(tb_ctx *ctx, int32_t natoms, const int32_t *g_rowptr, const int32_t *g_colidx,
                const double *g_vals, const double *q0);
 
+/* Build H, Gamma and q0 on the GPU from atom positions (bohr, 3*natoms) and
+ * species (14 Si, 8 O) in an orthorhombic box (box[d] > 0: periodic edge
+ * along d, 0: open), neighbours with 0.1 < d^2 < rcut^2 under the minimum
+ * image, the reference's sp3 block model, Gamma_aa = gamma_diag and 1/r off
+ * the diagonal, q0 = 4 (Si) / 6 (O) electrons.  Replaces getHaloAtoms +
+ * constructH + initializeForSCF (withSP2_deltaH.cpp:372-501, 969-1066,
+ * 854-899) and stands in for tb_set_hamiltonian + tb_set_scc.  Periodic
+ * edges must exceed 2 * rcut. */
+int tb_set_geometry(tb_ctx *ctx, int32_t natoms, const double *xyz, const int32_t *species,
+                    const double *box, double rcut_bohr, double gamma_diag);
+
 /* Gershgorin bounds of H + diag(shift) (shift may be NULL).
  * Replaces GershGorinParallel, withSP2_deltaH.cpp:144-209. */
 int tb_gershgorin(tb_ctx *ctx, const double *shift, double *lmin, double *lmax);

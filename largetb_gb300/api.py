@@ -131,6 +131,7 @@ def load(build_if_missing: bool = True):
     L.tb_get_params.argtypes = [_vp, C.POINTER(TbParams)]
     L.tb_set_hamiltonian.argtypes = [_vp, C.c_int32, _i32p, _i32p, _f64p, _i32p, C.c_int32]
     L.tb_set_scc.argtypes = [_vp, C.c_int32, _i32p, _i32p, _f64p, _f64p]
+    L.tb_set_geometry.argtypes = [_vp, C.c_int32, _f64p, _i32p, _f64p, C.c_double, C.c_double]
     L.tb_gershgorin.argtypes = [_vp, _vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.tb_density.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(TbReport)]
     L.tb_coulomb_shift.argtypes = [_vp, _f64p, _f64p]
@@ -305,6 +306,16 @@ class Context:
             self._h, self.natoms, np.ascontiguousarray(g_rowptr, np.int32),
             np.ascontiguousarray(g_colidx, np.int32), np.ascontiguousarray(g_vals, np.float64),
             np.ascontiguousarray(q0, np.float64)))
+
+    def set_geometry(self, xyz, species, box, rcut_bohr=4.0, gamma_diag=1.0):
+        """H, Gamma and q0 built on the GPU from positions (bohr) and species."""
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+        species = np.ascontiguousarray(species, np.int32)
+        self._check(self._L.tb_set_geometry(self._h, species.shape[0], xyz, species,
+                                            np.ascontiguousarray(box, np.float64), rcut_bohr,
+                                            gamma_diag))
+        self.natoms = int(species.shape[0])
+        self.n = 4 * self.natoms
 
     def set_model(self, m: Model, scc: bool = True):
         self.set_hamiltonian(m.rowptr, m.colidx, m.vals, m.orb2atom, m.natoms)

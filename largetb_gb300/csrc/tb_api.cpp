@@ -1021,6 +1021,72 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
     return TB_OK;
 }
 
+int tb_set_geometry(tb_ctx *ctx, int32_t natoms, const double *xyz, const int32_t *species,
+                    const double *box, double rcut_bohr, double gamma_diag)
+{
+    if (!ctx) return TB_ERR_INVALID_ARG;
+    if (natoms <= 0 || !xyz || !species || !box || !(rcut_bohr > 0) || !std::isfinite(gamma_diag))
+        return fail(ctx, TB_ERR_INVALID_ARG, "bad geometry arguments");
+    for (int d = 0; d < 3; d++) {
+        if (!(box[d] >= 0) || !std::isfinite(box[d])) return fail(ctx, TB_ERR_INVALID_ARG, "bad box");
+        if (box[d] > 0 && box[d] <= 2.0 * rcut_bohr)
+            return fail(ctx, TB_ERR_INVALID_ARG, "periodic box edges must exceed 2 * rcut (one image per pair)");
+    }
+    for (int i = 0; i < natoms; i++) {
+        if (species[i] != 14 && species[i] != 8)
+            return fail(ctx, TB_ERR_STRUCTURE, "species must be 14 (Si) or 8 (O)");
+        for (int d = 0; d < 3; d++)
+            if (!std::isfinite(xyz[3 * i + d])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in positions");
+    }
+    TB_TRY(set_device(ctx));
+    free_all(ctx);
+    ctx->have_h = ctx->have_scc = false;
+    ctx->tuned[0] = ctx->tuned[1] = 0;
+    GeomDevice g;
+    const int rc = geom_build_device(ctx->stream, natoms, xyz, species, box, rcut_bohr, gamma_diag, g, ctx->err);
+    DevMatrix &m = ctx->m;
+    m.rowptr = g.rowptr;
+    m.colidx = g.colidx;
+    m.blkrow = g.blkrow;
+    m.diagblk = g.diagblk;
+    m.h0 = g.h0;
+    m.h0diag = g.h0diag;
+    m.radius = g.radius;
+    DevScc &sc = ctx->s;
+    sc.val = g.gval;
+    sc.q0 = g.q0;
+    if (rc) return rc;
+    m.n = 4 * natoms;
+    m.natoms = m.nb = natoms;
+    m.nnzb = g.nnzb;
+    TB_TRY(dalloc(ctx, m.xdiag32, (size_t)m.n));
+    sc.natoms = natoms;
+    sc.nnz = g.nnzb;
+    TB_TRY(upload(ctx, sc.rowptr, g.brow.data(), g.brow.size()));
+    TB_TRY(upload(ctx, sc.colidx, g.bcol.data(), g.bcol.size()));
+    TB_TRY(dalloc(ctx, sc.qin, (size_t)natoms));
+    TB_TRY(dalloc(ctx, sc.qout, (size_t)natoms));
+    TB_TRY(dalloc(ctx, sc.V, (size_t)natoms));
+    TB_TRY(dalloc(ctx, sc.hist_q, (size_t)kMaxHistory * natoms));
+    TB_TRY(dalloc(ctx, sc.hist_r, (size_t)kMaxHistory * natoms));
+    TB_TRY(dalloc(ctx, sc.hist_meta, 2));
+    TB_TRY(build_stage_plan(ctx, g.brow, g.bcol));
+    TB_TRY(build_persist_plan(ctx, g.brow, g.bcol));
+    double mn = 1e300, mx = -1e300, ne = 0.0;
+    for (int i = 0; i < m.n; i++) {
+        mn = std::min(mn, g.h0diag_h[i] - g.radius_h[i]);
+        mx = std::max(mx, g.h0diag_h[i] + g.radius_h[i]);
+    }
+    for (int i = 0; i < natoms; i++) ne += species[i] == 14 ? 4.0 : 6.0;
+    ctx->h0_lmin = mn;
+    ctx->h0_lmax = mx;
+    if (!(ctx->p.n_electrons > 0)) ctx->p.n_electrons = ne;
+    ctx->asym_max = 0.0;
+    TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->have_h = ctx->have_scc = true;
+    return TB_OK;
+}
+
 int tb_set_scc(tb_ctx *ctx, int32_t natoms, const int32_t *g_rowptr, const int32_t *g_colidx,
                const double *g_vals, const double *q0)
 {

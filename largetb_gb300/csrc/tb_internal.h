@@ -186,6 +186,18 @@ int host_csr_to_bsr(int32_t n, const int32_t *rowptr, const int32_t *colidx, con
 int host_check_gamma(int32_t natoms, const int32_t *g_rowptr, const int32_t *g_colidx,
                      const double *g_vals, const double *q0, std::string &err);
 
+// ---- tb_geom.cu ----------------------------------------------------------
+struct GeomDevice {
+    int64_t nnzb = 0;
+    int32_t *rowptr = nullptr, *colidx = nullptr, *blkrow = nullptr, *diagblk = nullptr;
+    double *h0 = nullptr, *h0diag = nullptr, *radius = nullptr, *gval = nullptr, *q0 = nullptr;
+    std::vector<int32_t> brow, bcol;
+    std::vector<double> h0diag_h, radius_h;
+};
+int geom_build_device(cudaStream_t st, int natoms, const double *xyz_h, const int32_t *sp_h,
+                      const double box[3], double rcut, double gamma_diag, GeomDevice &out,
+                      std::string &err);
+
 // ---- tb_sp2.cu ----------------------------------------------------------
 // SP2 purification of the context's H; branches_out (optional) receives the
 // applied branch sequence (-1: X^2, +1: 2X - X^2).

@@ -257,6 +257,17 @@ def _finish(xyz, sp, cell, periodic, rcut2, rmin2, maxnb, gamma_diag):
                  col, val, g_rowptr, g_col, g_val, q0, orb2atom)
 
 
+def model_from_csr(rowptr, col, val, natoms):
+    """An oracle Model around given CSR arrays (H only: no geometry/Gamma)."""
+    nat = int(natoms)
+    e = np.zeros(0)
+    return Model(np.zeros((nat, 3)), np.zeros(nat, np.int32), np.zeros((3, 3)), np.zeros(nat, np.int32),
+                 np.zeros(0, np.int32), e, 0, np.ascontiguousarray(rowptr, np.int32),
+                 np.ascontiguousarray(col, np.int32), np.ascontiguousarray(val, np.float64),
+                 np.zeros(nat + 1, np.int32), np.zeros(0, np.int32), e, np.zeros(nat),
+                 np.repeat(np.arange(nat, dtype=np.int32), 4))
+
+
 def hblock(zi, zj, x, y, z):
     out = np.zeros(16)
     _check(lib().orc_hblock(zi, zj, x, y, z, out), "hblock")
