@@ -235,6 +235,41 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
 
 const char *tb_batch_last_error(const tb_batch *b);
 
+/* ------------------------------------------------------------------------ */
+/* Learned SCC starting charges (no counterpart in the reference, which      */
+/* starts every SCC loop from the neutral charges, withSP2_deltaH.cpp:1725)  */
+/* ------------------------------------------------------------------------ */
+#define TB_MLP_NFEAT 32
+#define TB_MLP_NPARAM 6337 /* W1[64][32] b1[64] W2[64][64] b2[64] w3[64] b3 */
+
+/* Per-atom radial features on the current device: for each atom, 16
+ * Gaussians exp(-12.5 (r - mu_k)^2) (r in angstrom, mu_k = 0.8 + 0.28 k) times
+ * the cosine cutoff (cos(pi r / 5) + 1)/2, summed over Si neighbours within
+ * 5 A, then 16 over O neighbours; minimum image in an orthorhombic box
+ * (edges in bohr, 0 = open).  feat is natoms x 32, row-major. */
+int tb_mlp_features(int32_t natoms, const double *xyz, const int32_t *species, const double *box,
+                    float *feat);
+
+/* A 32 -> 64 -> 64 -> 1 SiLU network predicting each atom's net charge
+ * q - q0 from its features; BF16 weights (rounded from FP32 masters), FP32
+ * activations and accumulation, trained by minibatch Adam on the mean
+ * squared error -- all on the GPU. */
+typedef struct tb_mlp tb_mlp;
+int tb_mlp_create(int32_t device, uint64_t seed, tb_mlp **out);
+int tb_mlp_destroy(tb_mlp *m);
+/* FP32 master parameters (TB_MLP_NPARAM) and the feature normalisation
+ * (mean[32], 1/std[32]); either pointer may be NULL. */
+int tb_mlp_get(const tb_mlp *m, float *params, float *norm);
+int tb_mlp_set(tb_mlp *m, const float *params, const float *norm);
+/* Train for `epochs` over n samples (the normalisation is fixed from the
+ * first training set unless set before); loss_per_epoch (may be NULL). */
+int tb_mlp_train(tb_mlp *m, int32_t n, const float *feat, const float *target, int32_t epochs,
+                 int32_t batch, float lr, uint64_t seed, float *loss_per_epoch);
+int tb_mlp_predict(tb_mlp *m, int32_t n, const float *feat, float *out);
+/* Gradient of the mean squared error w.r.t. the (BF16-rounded) parameters. */
+int tb_mlp_grad(tb_mlp *m, int32_t n, const float *feat, const float *target, float *grad,
+                float *loss);
+
 /* Message of the last failure on ctx (never NULL). */
 const char *tb_last_error(const tb_ctx *ctx);
 const char *tb_status_string(int status);

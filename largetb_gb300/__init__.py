@@ -5,7 +5,7 @@ The product is the C-ABI shared library built from ``largetb_gb300/csrc``
 exposes it to Python through ctypes (``largetb_gb300.api``).
 """
 from .api import (  # noqa: F401
-    Batch, Context, Model, TbError, TbParams, TbReport, load, model_cristobalite, model_quartz, params,
+    MLP, Batch, Context, Model, TbError, mlp_features, TbParams, TbReport, load, model_cristobalite, model_quartz, params,
     PREC_FP32, PREC_FP64, KERNEL_AUTOCORR, KERNEL_JACKSON, KERNEL_NONE,
 )
 from .build import build as build_library  # noqa: F401

@@ -157,6 +157,16 @@ def load(build_if_missing: bool = True):
     L.tb_batch_scc_solve.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(TbReport)]
     L.tb_batch_last_error.argtypes = [_vp]
     L.tb_batch_last_error.restype = C.c_char_p
+    _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+    L.tb_mlp_features.argtypes = [C.c_int32, _f64p, _i32p, _f64p, _f32p]
+    L.tb_mlp_create.argtypes = [C.c_int32, C.c_uint64, C.POINTER(_vp)]
+    L.tb_mlp_destroy.argtypes = [_vp]
+    L.tb_mlp_get.argtypes = [_vp, _vp, _vp]
+    L.tb_mlp_set.argtypes = [_vp, _vp, _vp]
+    L.tb_mlp_train.argtypes = [_vp, C.c_int32, _f32p, _f32p, C.c_int32, C.c_int32, C.c_float,
+                               C.c_uint64, _vp]
+    L.tb_mlp_predict.argtypes = [_vp, C.c_int32, _f32p, _f32p]
+    L.tb_mlp_grad.argtypes = [_vp, C.c_int32, _f32p, _f32p, _f32p, _vp]
     _lib = L
     return L
 
@@ -435,3 +445,80 @@ class Batch:
         offs = np.cumsum([0] + self.natoms)
         return dict(status=rc, q=[q[offs[i]:offs[i + 1]] for i in range(S)], iters=it, e_band=eb,
                     mu=mu, report=rep.as_dict())
+
+
+MLP_NFEAT = 32
+MLP_NPARAM = 6337
+
+
+def mlp_features(xyz, species, box):
+    """Per-atom radial features (tb_mlp_features), natoms x 32 float32."""
+    xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+    species = np.ascontiguousarray(species, np.int32)
+    out = np.zeros((species.shape[0], MLP_NFEAT), np.float32)
+    rc = load().tb_mlp_features(species.shape[0], xyz, species, np.ascontiguousarray(box, np.float64),
+                                out)
+    if rc:
+        raise TbError(rc, "tb_mlp_features failed")
+    return out
+
+
+class MLP:
+    """Per-atom charge model trained and evaluated on the GPU (tb_mlp_*)."""
+
+    def __init__(self, device=0, seed=1):
+        self._L = load()
+        h = _vp()
+        rc = self._L.tb_mlp_create(device, seed, C.byref(h))
+        if rc:
+            raise TbError(rc, "tb_mlp_create failed")
+        self._h = h
+
+    def _chk(self, rc, what):
+        if rc:
+            raise TbError(rc, what)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.tb_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get(self):
+        p = np.zeros(MLP_NPARAM, np.float32)
+        nrm = np.zeros(2 * MLP_NFEAT, np.float32)
+        self._chk(self._L.tb_mlp_get(self._h, _ptr(p), _ptr(nrm)), "tb_mlp_get")
+        return p, nrm
+
+    def set(self, params=None, norm=None):
+        p = None if params is None else np.ascontiguousarray(params, np.float32)
+        n = None if norm is None else np.ascontiguousarray(norm, np.float32)
+        self._chk(self._L.tb_mlp_set(self._h, _ptr(p), _ptr(n)), "tb_mlp_set")
+
+    def train(self, feat, target, epochs=10, batch=1024, lr=1e-3, seed=0):
+        feat = np.ascontiguousarray(feat, np.float32)
+        target = np.ascontiguousarray(target, np.float32)
+        loss = np.zeros(epochs, np.float32)
+        self._chk(self._L.tb_mlp_train(self._h, target.shape[0], feat, target, epochs, batch, lr, seed,
+                                       _ptr(loss)), "tb_mlp_train")
+        return loss
+
+    def predict(self, feat):
+        feat = np.ascontiguousarray(feat, np.float32)
+        out = np.zeros(feat.shape[0], np.float32)
+        self._chk(self._L.tb_mlp_predict(self._h, feat.shape[0], feat, out), "tb_mlp_predict")
+        return out
+
+    def grad(self, feat, target):
+        feat = np.ascontiguousarray(feat, np.float32)
+        target = np.ascontiguousarray(target, np.float32)
+        g = np.zeros(MLP_NPARAM, np.float32)
+        loss = np.zeros(1, np.float32)
+        self._chk(self._L.tb_mlp_grad(self._h, target.shape[0], feat, target, g, _ptr(loss)),
+                  "tb_mlp_grad")
+        return g, float(loss[0])
