@@ -246,6 +246,39 @@ def run_batch_bench(args, T, dev, rank):
                        "seed": 4004, "M": M, "kT": 0.01, "scc_tol": 1e-6}}), flush=True)
 
 
+def run_learned_eval(args, T, dev, rank):
+    """Learned SCC start on an 8x8x8 cell (12288 atoms, 49152 orbitals),
+    sigma 0.08 A, M = 200 (the training M), FP32 form: iterations and time to
+    |dq| < 1e-6 e from the neutral charges and from the MLP prediction."""
+    from largetb_gb300 import learned
+    cells = args.cells or [8, 8, 8]
+    m = T.model_cristobalite(*cells, sigma_ang=0.08, seed=8008)
+    mlp = learned.load(device=dev)
+    box = learned.cell_box(cells)
+    c = T.Context(M=200, precision=T.PREC_FP32, device=dev)
+    c.set_model(m)
+    c.density()  # slab-width autotune outside the timings
+    l2_flush(dev)
+    rz = c.scc_solve()
+    l2_flush(dev)
+    t = time.perf_counter()
+    q_init = learned.warm_start(mlp, m, box)
+    t_mlp = time.perf_counter() - t
+    rl = c.scc_solve(q_init=q_init)
+    c.close()
+    if rank == 0:
+        tz, tl = rz["report"]["t_total_ms"] / 1e3, rl["report"]["t_total_ms"] / 1e3 + t_mlp
+        print(json.dumps({"metric": "SCC iterations and s to |dq|<1e-6 e, 8x8x8 cristobalite",
+                          "config": {"cells": cells, "atoms": m.natoms, "orbitals": m.n, "sigma_ang": 0.08,
+                                     "seed": 8008, "M": 200, "precision": "fp32"},
+                          "zero_start": {"iters": rz["iters"], "s": tz},
+                          "learned_start": {"iters": rl["iters"], "s": tl, "mlp_s": t_mlp,
+                                            "start_err_max_e": float(np.abs(q_init - rz["q"]).max()),
+                                            "q0_err_max_e": float(np.abs(m.q0 - rz["q"]).max())},
+                          "speedup": tz / tl,
+                          "max_dq_between_solutions": float(np.abs(rz["q"] - rl["q"]).max())}), flush=True)
+
+
 def run_sp2_bench(args, T, dev, rank):
     """SP2 path: 4x4x4 beta-cristobalite (1536 atoms, 6144 orbitals), sigma
     0.08 A, Gershgorin X_0, drop 1e-5 on 4x4 blocks, <= 40 steps."""
@@ -291,6 +324,10 @@ def main():
     ap.add_argument("--column-block", type=int, default=0)
     ap.add_argument("--density-only", action="store_true",
                     help="time single density evaluations (the unit profiled with ncu)")
+    ap.add_argument("--zero-start", action="store_true",
+                    help="start the timed solves from q0 instead of the learned charges")
+    ap.add_argument("--learned-eval", action="store_true",
+                    help="8x8x8 cell (12288 atoms): SCC from q0 vs from the learned start (M = 200)")
     ap.add_argument("--batch", action="store_true",
                     help="64 cristobalite cells of random shape solved as one batch (M = 300)")
     ap.add_argument("--sp2", action="store_true",
@@ -311,6 +348,9 @@ def main():
         return
     if args.batch:
         run_batch_bench(args, T, dev, rank)
+        return
+    if args.learned_eval:
+        run_learned_eval(args, T, dev, rank)
         return
     cells = args.cells or WORKLOAD["cells"]
     cfg = dict(WORKLOAD)
@@ -344,9 +384,21 @@ def main():
                               "kernel_launches": ms[-1]["kernel_launches"]}), flush=True)
         return
 
+    from largetb_gb300 import learned
+    mlp = None if args.zero_start else learned.load(device=dev)
+    box = learned.cell_box(cells)
+
+    def start():
+        """Learned starting charges (features + MLP on the GPU) and their wall time."""
+        if mlp is None:
+            return None, 0.0
+        t = time.perf_counter()
+        q = learned.warm_start(mlp, m, box)
+        return q, time.perf_counter() - t
+
     for _ in range(args.warmup):
         l2_flush(dev)
-        ctx.scc_solve()
+        ctx.scc_solve(q_init=start()[0])
 
     clocks = Clocks(dev)
     barrier(ws)
@@ -356,9 +408,10 @@ def main():
     t0 = time.perf_counter()
     for _ in range(args.steps):
         l2_flush(dev)
-        r = ctx.scc_solve()
+        q_init, t_start = start()
+        r = ctx.scc_solve(q_init=q_init)
         rep = r["report"]
-        dev_ms.append(rep["t_total_ms"])
+        dev_ms.append(rep["t_total_ms"] + 1e3 * t_start)
         mom_ms.append(rep["t_moments_ms"])
         launches += rep["kernel_launches"]
         spmm_l += rep["spmm_launches"]
@@ -382,9 +435,14 @@ def main():
         l2_flush(dev)
         t1 = time.perf_counter()
         ctx.set_model(m)
-        r2 = ctx.scc_solve()
+        r2 = ctx.scc_solve(q_init=start()[0])
         e2e.append(time.perf_counter() - t1)
     barrier(ws)
+    # the same solve from the neutral charges (the reference's start)
+    l2_flush(dev)
+    rz = ctx.scc_solve()
+    zero = {"s_per_solve": rz["report"]["t_total_ms"] / 1e3, "iters": rz["iters"],
+            "max_dq_vs_learned_start": float(np.abs(rz["q"] - q32).max())}
 
     value = allmax(ws, statistics.mean(dev_ms) / 1e3)
     e2e_v = allmax(ws, statistics.mean(e2e))
@@ -402,6 +460,8 @@ def main():
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "scc_iterations": iters,
+        "start": "learned (MLP, largetb_gb300/data/charge_mlp.npz)" if mlp is not None else "neutral q0",
+        "zero_start_fp32": zero,
         "wall_s_per_step": wall / args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_source": src,
@@ -418,6 +478,7 @@ def main():
         r64 = ctx64.scc_solve()
         rep64 = r64["report"]
         line["plain_fp64"] = {"s_per_solve": rep64["t_total_ms"] / 1e3, "iters": r64["iters"],
+                              "start": "neutral q0",
                               "moments_s": rep64["t_moments_ms"] / 1e3,
                               "speedup_fast_vs_plain": rep64["t_total_ms"] / 1e3 / value,
                               "max_dq_fast_vs_plain": float(np.abs(q32 - r64["q"]).max()),
