@@ -322,6 +322,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--column-block", type=int, default=0)
+    ap.add_argument("--fp32-kernel", type=int, default=0,
+                    help="0 autotune, 1 staged, 2 persistent, 3 pipelined")
     ap.add_argument("--density-only", action="store_true",
                     help="time single density evaluations (the unit profiled with ncu)")
     ap.add_argument("--zero-start", action="store_true",
@@ -361,7 +363,7 @@ def main():
     cfg["atoms"], cfg["orbitals"] = m.natoms, m.n
     M = cfg["M"]
     ctx = T.Context(M=M, kT=cfg["kT"], precision=T.PREC_FP32, device=dev,
-                    column_block=args.column_block, scc_tol=cfg["scc_tol"])
+                    column_block=args.column_block, fp32_kernel=args.fp32_kernel, scc_tol=cfg["scc_tol"])
     ctx.set_model(m)
     if args.density_only:
         for _ in range(args.warmup):
@@ -381,6 +383,7 @@ def main():
                               statistics.mean(r["t_total_ms"] for r in ms) / 1e3, "unit": "s",
                               "config": cfg, "spmm_launches": nl, "spmm_GBps": b / tot / 1e9,
                               "avg_launch_us": tot * 1e6 / nl, "column_block": ms[-1]["column_block"],
+                              "step_kernel": ms[-1]["step_kernel"],
                               "kernel_launches": ms[-1]["kernel_launches"]}), flush=True)
         return
 
@@ -413,7 +416,7 @@ def main():
         rep = r["report"]
         dev_ms.append(rep["t_total_ms"] + 1e3 * t_start)
         mom_ms.append(rep["t_moments_ms"])
-        launches += rep["kernel_launches"]
+        launches += rep["kernel_launches"] + (2 if mlp is not None else 0)  # + k_features, k_mlp_fb
         spmm_l += rep["spmm_launches"]
         spmm_b += rep["spmm_bytes"]
         iters.append(r["iters"])

@@ -58,6 +58,16 @@ enum tb_precision {
                          from T_{2k} = 2 T_k^2 - 1, T_{2k+1} = 2 T_k T_{k+1} - X */
 };
 
+/* Chebyshev step kernel of the FP32 form (tb_params.fp32_kernel).  No
+ * counterpart in the reference, whose recurrence is PETSc's MatMult. */
+enum tb_fp32_kernel {
+    TB_FP32_AUTO = 0,       /* autotuner picks kernel and slab width (column_block = 0);
+                               with column_block set: pipelined where it fits, else staged */
+    TB_FP32_STAGED = 1,     /* one launch per step, row-group staging in shared memory */
+    TB_FP32_PERSISTENT = 2, /* one cooperative launch per slab, neighbour-synchronised */
+    TB_FP32_PIPELINED = 3   /* one launch per step, SM-resident CTAs with a bulk-copy stage ring */
+};
+
 enum tb_kernel_kind {
     TB_KERNEL_JACKSON = 0,  /* closed form of runKPM, withSP2_deltaH.cpp:1593-1595 */
     TB_KERNEL_AUTOCORR = 1, /* getKPE's autocorrelation form, withSP2_deltaH.cpp:1104-1132 */
@@ -86,7 +96,7 @@ typedef struct tb_params {
     double mix_beta;       /* mixing parameter */
     double sp2_drop_tol;   /* SP2: drop 4x4 blocks with Frobenius norm below this */
     int32_t sp2_max_iter;
-    int32_t reserved0;
+    int32_t fp32_kernel;   /* enum tb_fp32_kernel */
     double sp2_idem_tol;   /* SP2: stop when ||X^2 - X||_F < sp2_idem_tol */
     double reserved[6];
 } tb_params;
@@ -110,7 +120,7 @@ typedef struct tb_report {
     double asym_max;          /* max |H_ij - H_ji| seen by tb_set_hamiltonian */
     double idem_err;          /* SP2: ||X^2 - X||_F of the returned X */
     int32_t sp2_iters;
-    int32_t reserved0;
+    int32_t step_kernel;      /* FP32 form: enum tb_fp32_kernel actually used */
     int64_t sp2_nnzb;         /* SP2: stored blocks of the returned X */
     double reserved[8];
 } tb_report;

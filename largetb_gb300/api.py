@@ -40,6 +40,10 @@ PREC_FP32 = 1
 KERNEL_JACKSON = 0
 KERNEL_AUTOCORR = 1
 KERNEL_NONE = 2
+FP32_AUTO = 0
+FP32_STAGED = 1
+FP32_PERSISTENT = 2
+FP32_PIPELINED = 3
 
 
 class TbParams(C.Structure):
@@ -60,7 +64,7 @@ class TbParams(C.Structure):
         ("mix_beta", C.c_double),
         ("sp2_drop_tol", C.c_double),
         ("sp2_max_iter", C.c_int32),
-        ("reserved0", C.c_int32),
+        ("fp32_kernel", C.c_int32),
         ("sp2_idem_tol", C.c_double),
         ("reserved", C.c_double * 6),
     ]
@@ -88,7 +92,7 @@ class TbReport(C.Structure):
         ("asym_max", C.c_double),
         ("idem_err", C.c_double),
         ("sp2_iters", C.c_int32),
-        ("reserved0", C.c_int32),
+        ("step_kernel", C.c_int32),
         ("sp2_nnzb", C.c_int64),
         ("reserved", C.c_double * 8),
     ]

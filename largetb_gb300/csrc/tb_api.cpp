@@ -124,6 +124,8 @@ int check_params(tb_ctx *ctx, const tb_params *p)
         return fail(ctx, TB_ERR_INVALID_ARG, "bad pad / tolerance / iteration cap");
     if (p->mix_history < 0 || p->mix_history > kMaxHistory || !(p->mix_beta > 0))
         return fail(ctx, TB_ERR_INVALID_ARG, "mix_history must be in [0,16], mix_beta > 0");
+    if (p->fp32_kernel < TB_FP32_AUTO || p->fp32_kernel > TB_FP32_PIPELINED)
+        return fail(ctx, TB_ERR_INVALID_ARG, "unknown fp32_kernel");
     if (!(p->sp2_drop_tol >= 0) || p->sp2_max_iter < 1 || !(p->sp2_idem_tol >= 0))
         return fail(ctx, TB_ERR_INVALID_ARG, "bad SP2 parameters");
     return TB_OK;
@@ -137,30 +139,68 @@ int set_device(tb_ctx *ctx)
 
 double step_bytes(const DevMatrix &m, int B, int s);
 
+void reset_tuning(tb_ctx *ctx)
+{
+    for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 4; b++) ctx->tuned_kind[a][b] = ctx->tuned_B[a][b] = 0;
+}
+
+// Error flags raised by the bounded waits of the persistent and pipelined
+// step kernels; synchronises the stream.
+int check_kernel_flags(tb_ctx *ctx)
+{
+    int32_t perr = 0, serr = 0;
+    if (ctx->pp.err)
+        TB_CUDA(cudaMemcpyAsync(&perr, ctx->pp.err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    if (ctx->pl.err)
+        TB_CUDA(cudaMemcpyAsync(&serr, ctx->pl.err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (perr) {
+        cudaMemsetAsync(ctx->pp.err, 0, sizeof(int32_t), ctx->stream);
+        return fail(ctx, TB_ERR_CUDA, "persistent Chebyshev kernel: neighbour wait timed out");
+    }
+    if (serr) {
+        cudaMemsetAsync(ctx->pl.err, 0, sizeof(int32_t), ctx->stream);
+        return fail(ctx, TB_ERR_CUDA, "pipelined Chebyshev kernel: stage wait timed out");
+    }
+    return TB_OK;
+}
+
 // Slab-width autotuner (column_block = 0): time kTuneSteps Chebyshev steps of
 // one slab for every candidate kernel/width on this matrix and keep the one
-// with the least time per identity column.  Runs once per matrix and
-// precision; the X used is the unshifted one.
-int autotune(tb_ctx *ctx)
+// with the least time per identity column.  Runs once per matrix, precision
+// and requested FP32 kernel (req, a StepKind; kKindAuto tries them all); the
+// X used is the unshifted one.
+int autotune(tb_ctx *ctx, int req)
 {
     constexpr int kTuneSteps = 12;
     DevMatrix &m = ctx->m;
     cudaStream_t st = ctx->stream;
     const int prec = ctx->p.precision;
-    const int nround = ((m.n + 63) / 64) * 64;
+    const int n64 = ((m.n + 63) / 64) * 64, n128 = ((m.n + 127) / 128) * 128;
     struct Cand {
-        bool persist;
+        int kind;
         int B;
     };
     std::vector<Cand> cands;
+    auto widths = [&](int kind, std::initializer_list<int> Bs, int q) {
+        const int nr = q == 128 ? n128 : n64;
+        for (int B : Bs) {
+            const int Bc = std::min(B, nr);
+            bool dup = false;
+            for (const Cand &c : cands) dup |= (c.kind == kind && c.B == Bc);
+            if (!dup) cands.push_back({kind, Bc});
+        }
+    };
     if (prec == TB_PREC_FP32) {
-        if (ctx->pp.R > 0) cands.push_back({true, ctx->pp.B});
-        for (int B : {256, 384, 512})
-            if (B <= ((m.n + 127) / 128) * 128 || B == 256) cands.push_back({false, std::min(B, ((m.n + 127) / 128) * 128)});
+        if ((req == kKindAuto || req == kKindPersistent) && ctx->pp.R > 0) cands.push_back({kKindPersistent, ctx->pp.B});
+        if ((req == kKindAuto || req == kKindPipelined) && ctx->pl.stages > 0)
+            widths(kKindPipelined, {256, 512, 1024}, 64);
+        if (req == kKindAuto || req == kKindStaged) widths(kKindStaged, {256, 384, 512}, ctx->sp.R > 0 ? 64 : 128);
     } else {
-        for (int B : {64, 128, 256})
-            if (B <= nround || B == 64) cands.push_back({false, std::min(B, ((m.n + 63) / 64) * 64)});
+        widths(kKindStaged, {64, 128, 256}, 64);
     }
+    if (cands.empty()) return fail(ctx, TB_ERR_UNSUPPORTED, "requested FP32 step kernel has no plan for this matrix");
     DevState *state = nullptr;
     TB_TRY(dalloc(ctx, state, 1));
     if (prec == TB_PREC_FP32 && !m.x32) TB_TRY(dalloc(ctx, m.x32, (size_t)m.nnzb * 16));
@@ -175,7 +215,9 @@ int autotune(tb_ctx *ctx)
     for (const Cand &cd : cands) {
         const int B = cd.B;
         const size_t es = prec == TB_PREC_FP32 ? 4 : 8;
-        const int rowgroups = cd.persist ? ctx->pp.G : (ctx->sp.R > 0 ? ctx->sp.G : cheb_f32_rowgroups(m.nb));
+        const int rowgroups = cd.kind == kKindPersistent   ? ctx->pp.G
+                              : cd.kind == kKindPipelined ? ctx->pl.G
+                                                          : (ctx->sp.R > 0 ? ctx->sp.G : cheb_f32_rowgroups(m.nb));
         char *T0 = nullptr, *T1 = nullptr;
         double *part = nullptr, *dd = nullptr;
         TB_TRY(dalloc(ctx, T0, (size_t)m.n * B * es));
@@ -187,23 +229,28 @@ int autotune(tb_ctx *ctx)
         float ms = 0.f;
         for (int rep = 0; rep < 2; rep++) {  // the first pass warms up
             cudaEventRecord(a, st);
-            if (cd.persist) {
+            if (cd.kind == kKindPersistent) {
                 cudaMemsetAsync(ctx->pp.flags, 0, sizeof(int32_t) * ctx->pp.G * ctx->pp.nc, st);
                 launch_cheb_f32_persistent(st, m, ctx->pp, kTuneSteps, B, 0, (float *)T0, (float *)T1, part,
                                            ctx->pp.flags, ctx->pp.err);
             } else {
-                launch_slab_identity(st, T0, m.n, B, 0, prec);
+                if (cd.kind == kKindPipelined)
+                    launch_slab_identity_cm(st, (float *)T0, m.n, B, 0);
+                else
+                    launch_slab_identity(st, T0, m.n, B, 0, prec);
                 for (int k = 0; k < kTuneSteps; k++) {
                     const bool odd = (k + 1) & 1;
                     char *in = odd ? T0 : T1, *out = odd ? T1 : T0;
+                    double *pk = part ? part + (int64_t)k * rowgroups * B * 2 : nullptr;
                     if (prec == TB_PREC_FP64)
                         launch_cheb_step_f64(st, m, (double *)in, (double *)out, B, 0, k == 0, dd, k + 1);
+                    else if (cd.kind == kKindPipelined)
+                        launch_cheb_step_f32_pipe(st, m, ctx->pl, (float *)in, (float *)out, B, k == 0,
+                                                  reinterpret_cast<float2 *>(pk));
                     else if (ctx->sp.R > 0)
-                        launch_cheb_step_f32_staged(st, m, ctx->sp, (float *)in, (float *)out, B, k == 0,
-                                                    part + (int64_t)k * rowgroups * B * 2);
+                        launch_cheb_step_f32_staged(st, m, ctx->sp, (float *)in, (float *)out, B, k == 0, pk);
                     else
-                        launch_cheb_step_f32(st, m, (float *)in, (float *)out, B, k == 0,
-                                             part + (int64_t)k * rowgroups * B * 2, rowgroups);
+                        launch_cheb_step_f32(st, m, (float *)in, (float *)out, B, k == 0, pk, rowgroups);
                 }
             }
             cudaEventRecord(b, st);
@@ -224,7 +271,9 @@ int autotune(tb_ctx *ctx)
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     dfree(state);
-    ctx->tuned[prec] = pick.persist ? -1 : pick.B;
+    TB_TRY(check_kernel_flags(ctx));
+    ctx->tuned_kind[prec][req] = pick.kind;
+    ctx->tuned_B[prec][req] = pick.B;
     return TB_OK;
 }
 
@@ -235,31 +284,43 @@ int ensure_work(tb_ctx *ctx)
     const DevMatrix &m = ctx->m;
     const tb_params &p = ctx->p;
     const int M = p.M;
-    if (p.column_block == 0 && ctx->tuned[p.precision] == 0) TB_TRY(autotune(ctx));
-    const int tuned = ctx->tuned[p.precision];
-    const bool persist = p.precision == TB_PREC_FP32 && ctx->pp.R > 0 && p.column_block == 0 && tuned < 0;
-    int B = p.column_block;
-    if (persist)
+    const int prec = p.precision;
+    const int req = prec == TB_PREC_FP32 ? p.fp32_kernel : kKindAuto;
+    int kind = kKindStaged, B = p.column_block;
+    if (B == 0) {
+        if (ctx->tuned_B[prec][req] == 0) TB_TRY(autotune(ctx, req));
+        kind = ctx->tuned_kind[prec][req];
+        B = ctx->tuned_B[prec][req];
+    } else if (prec == TB_PREC_FP32) {
+        kind = req != kKindAuto ? req : (ctx->pl.stages > 0 ? kKindPipelined : kKindStaged);
+    }
+    if (kind == kKindPersistent && ctx->pp.R == 0)
+        return fail(ctx, TB_ERR_UNSUPPORTED, "persistent FP32 kernel: no task plan fits this matrix");
+    if (kind == kKindPipelined && ctx->pl.stages == 0)
+        return fail(ctx, TB_ERR_UNSUPPORTED, "pipelined FP32 kernel: no stage plan fits this matrix");
+    if (kind == kKindPersistent) {
         B = ctx->pp.B;
-    else {
-        if (B == 0) B = tuned > 0 ? tuned : ((p.precision == TB_PREC_FP32) ? 256 : 128);
+    } else {
         // the unstaged FP32 kernel works in 128-column chunks, the others in 64
-        const int q = (p.precision == TB_PREC_FP32 && ctx->sp.R == 0) ? 128 : 64;
+        const int q = (prec == TB_PREC_FP32 && ctx->sp.R == 0) ? 128 : 64;
         const int nround = ((m.n + q - 1) / q) * q;
         if (B > nround) B = nround;
     }
-    const int K = (p.precision == TB_PREC_FP32) ? (M + 2) / 2 : 0;
-    const int rowgroups = (p.precision == TB_PREC_FP32)
-                              ? (persist ? ctx->pp.G : (ctx->sp.R > 0 ? ctx->sp.G : cheb_f32_rowgroups(m.nb)))
-                              : 0;
-    w.persist = persist;
+    const bool persist = kind == kKindPersistent;
+    const int K = (prec == TB_PREC_FP32) ? (M + 2) / 2 : 0;
+    const int rowgroups = (prec != TB_PREC_FP32)       ? 0
+                          : persist                      ? ctx->pp.G
+                          : kind == kKindPipelined       ? ctx->pl.G
+                          : ctx->sp.R > 0                ? ctx->sp.G
+                                                         : cheb_f32_rowgroups(m.nb);
+    w.kind = kind;
     // quadrature capacity from the Gershgorin width of H0 with a 2x margin
     // for SCC shifts; the device flags TB_ERR_SPECTRUM if it is exceeded.
     int nq_cap = 1 << 14;
     if (p.kT > 0)
         nq_cap = std::max(nq_cap, quad_nodes(M, 2.0 * (ctx->h0_lmax - ctx->h0_lmin) / p.kT));
     const bool same = w.M == M && w.B == B && w.K == K && w.precision == p.precision &&
-                      w.persist == persist &&
+                      w.kind == kind &&
                       w.rowgroups == rowgroups && w.nq_cap >= nq_cap && w.d && w.mom && w.T0 &&
                       w.kernel == p.kernel;
     if (same) return TB_OK;
@@ -400,6 +461,109 @@ int build_stage_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::v
     return TB_OK;
 }
 
+// Plan of the pipelined FP32 kernel: R is the candidate with the least
+// estimated step traffic (distinct referenced rows plus own T_{k-1} rows,
+// divided by the wave efficiency of 512-column slabs on one CTA per SM) among
+// those whose stage fits a ring of three (else two) stages in 227 KB.
+int build_pipe_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::vector<int32_t> &bcol)
+{
+    PipePlan &pl = ctx->pl;
+    dfree(pl.hdr);
+    dfree(pl.runs);
+    dfree(pl.rec);
+    dfree(pl.err);
+    pl = PipePlan{};
+    const int nb = (int)brow.size() - 1;
+    int nsm = 152;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+    std::vector<int32_t> mark(nb, -1);
+    struct Pick {
+        int R = 0, stages = 0;
+        double cost = 1e300;
+    } best;
+    for (int R : {12, 16, 20, 24, 28, 32}) {
+        const int G = (nb + R - 1) / R;
+        int64_t tot = 0;
+        int maxU = 0, maxBlk = 0;
+        for (int g = 0; g < G; g++) {
+            const int I0 = g * R, I1 = std::min(nb, I0 + R);
+            int u = 0;
+            for (int t = brow[I0]; t < brow[I1]; t++)
+                if (mark[bcol[t]] != g) {
+                    mark[bcol[t]] = g;
+                    u++;
+                }
+            tot += u;
+            maxU = std::max(maxU, u);
+            maxBlk = std::max(maxBlk, brow[I1] - brow[I0]);
+        }
+        std::fill(mark.begin(), mark.end(), -1);
+        const int rec_cap = ((2 * R + 1 + maxBlk) + 3) / 4 * 4;
+        const size_t stage = cheb_f32_pipe_stage_bytes(R, maxU, maxBlk, rec_cap);
+        int stages = 3;
+        while (stages >= 2 && cheb_f32_pipe_smem(stage, stages) > 227 * 1024) stages--;
+        if (stages < 2) continue;
+        const int64_t tiles = (int64_t)G * 8;
+        const double eff = (double)tiles / (double)(((tiles + nsm - 1) / nsm) * nsm);
+        const double cost = (double)(tot + nb) / eff * (stages == 3 ? 1.0 : 1.25);
+        if (cost < best.cost) best = {R, stages, cost};
+    }
+    if (best.R == 0) return TB_OK;  // pipelined kernel unavailable for this matrix
+    const int R = best.R, G = (nb + R - 1) / R;
+    std::vector<int32_t> hdr((size_t)G * 8, 0), runs, rec;
+    int maxU = 0, maxBlk = 0, rec_cap = 0;
+    for (int g = 0; g < G; g++) {
+        const int I0 = g * R, I1 = std::min(nb, I0 + R), tb0 = brow[I0];
+        std::vector<int32_t> U(bcol.begin() + tb0, bcol.begin() + brow[I1]);
+        std::sort(U.begin(), U.end());
+        U.erase(std::unique(U.begin(), U.end()), U.end());
+        const int nu = (int)U.size();
+        const size_t rstart = rec.size(), run0 = runs.size() / 4;
+        for (int I = I0; I <= I1; I++) rec.push_back(brow[I] - tb0);
+        for (int t = tb0; t < brow[I1]; t++)
+            rec.push_back((int32_t)(std::lower_bound(U.begin(), U.end(), bcol[t]) - U.begin()));
+        for (int I = I0; I < I1; I++) rec.push_back((int32_t)(std::lower_bound(U.begin(), U.end(), I) - U.begin()));
+        while ((rec.size() - rstart) % 4) rec.push_back(0);
+        for (int k = 0; k < nu;) {
+            int e = k + 1;
+            while (e < nu && U[e] == U[e - 1] + 1) e++;
+            runs.insert(runs.end(), {U[k], e - k, k, 0});
+            k = e;
+        }
+        int32_t *h = &hdr[(size_t)g * 8];
+        h[0] = nu;
+        h[1] = tb0;
+        h[2] = brow[I1] - tb0;
+        h[3] = (int32_t)rstart;
+        h[4] = (int32_t)(rec.size() - rstart);
+        h[5] = (int32_t)run0;
+        h[6] = (int32_t)(runs.size() / 4 - run0);
+        h[7] = I1 - I0;
+        maxU = std::max(maxU, nu);
+        maxBlk = std::max(maxBlk, h[2]);
+        rec_cap = std::max(rec_cap, h[4]);
+    }
+    const size_t stage_bytes = cheb_f32_pipe_stage_bytes(R, maxU, maxBlk, rec_cap);
+    const size_t smem = cheb_f32_pipe_smem(stage_bytes, best.stages);
+    if (smem > 227 * 1024 || cheb_f32_pipe_configure(smem) != (int)cudaSuccess) {
+        cudaGetLastError();
+        return TB_OK;
+    }
+    TB_TRY(upload(ctx, pl.hdr, hdr.data(), hdr.size()));
+    TB_TRY(upload(ctx, pl.runs, runs.data(), runs.size()));
+    TB_TRY(upload(ctx, pl.rec, rec.data(), rec.size()));
+    TB_TRY(dalloc(ctx, pl.err, 1));
+    TB_CUDA(cudaMemsetAsync(pl.err, 0, sizeof(int32_t), ctx->stream));
+    pl.R = R;
+    pl.G = G;
+    pl.maxU = maxU;
+    pl.maxBlk = maxBlk;
+    pl.stages = best.stages;
+    pl.stage_bytes = stage_bytes;
+    pl.nsm = nsm;
+    return TB_OK;
+}
+
 // Task plan of the persistent FP32 kernel: row groups of R block rows, each
 // with its halo (referenced rows owned by other groups) and its neighbouring
 // groups; nc 64-column chunks per slab so that all G * nc tasks are resident
@@ -537,7 +701,10 @@ int density_eval(tb_ctx *ctx, bool have_shift)
     const int nslab = (m.n + B - 1) / B;
     for (int s = 0; s < nslab; s++) {
         const int c0 = s * B;
-        if (!w.persist) {
+        if (w.kind == kKindPipelined) {
+            launch_slab_identity_cm(st, (float *)w.T0, m.n, B, c0);
+            ctx->launches++;
+        } else if (w.kind != kKindPersistent) {
             launch_slab_identity(st, w.T0, m.n, B, c0, p.precision);
             ctx->launches++;
         }
@@ -550,7 +717,7 @@ int density_eval(tb_ctx *ctx, bool have_shift)
             }
             ctx->spmm_launches += M;
             ctx->spmm_bytes += M * step_bytes(m, B, 8);
-        } else if (w.persist) {
+        } else if (w.kind == kKindPersistent) {
             TB_CUDA(cudaMemsetAsync(ctx->pp.flags, 0, sizeof(int32_t) * ctx->pp.G * ctx->pp.nc, st));
             const int e = launch_cheb_f32_persistent(st, m, ctx->pp, w.K, B, c0, (float *)w.T0,
                                                      (float *)w.T1, w.partial, ctx->pp.flags,
@@ -568,13 +735,20 @@ int density_eval(tb_ctx *ctx, bool have_shift)
                 const int kout = k + 1;
                 const bool odd = kout & 1;
                 double *pk = w.partial + (int64_t)k * w.rowgroups * B * 2;
-                if (ctx->sp.R > 0)
+                if (w.kind == kKindPipelined)
+                    launch_cheb_step_f32_pipe(st, m, ctx->pl, odd ? A : Bf, odd ? Bf : A, B, k == 0,
+                                              reinterpret_cast<float2 *>(pk));
+                else if (ctx->sp.R > 0)
                     launch_cheb_step_f32_staged(st, m, ctx->sp, odd ? A : Bf, odd ? Bf : A, B, k == 0, pk);
                 else
                     launch_cheb_step_f32(st, m, odd ? A : Bf, odd ? Bf : A, B, k == 0, pk, w.rowgroups);
                 ctx->launches++;
             }
-            launch_f32_finalize(st, m, w.partial, w.K, w.rowgroups, B, c0, w.d, M);
+            if (w.kind == kKindPipelined)
+                launch_f32_finalize_pairs(st, m, reinterpret_cast<const float2 *>(w.partial), w.K, w.rowgroups, B,
+                                          c0, w.d, M);
+            else
+                launch_f32_finalize(st, m, w.partial, w.K, w.rowgroups, B, c0, w.d, M);
             ctx->launches++;
             ctx->spmm_launches += w.K;
             ctx->spmm_bytes += w.K * step_bytes(m, B, 4);
@@ -602,16 +776,8 @@ int density_eval(tb_ctx *ctx, bool have_shift)
 
 int read_state(tb_ctx *ctx, DevState &hs)
 {
-    int32_t perr = 0;
     TB_CUDA(cudaMemcpyAsync(&hs, ctx->w.state, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
-    if (ctx->pp.err)
-        TB_CUDA(cudaMemcpyAsync(&perr, ctx->pp.err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
-    TB_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (perr) {
-        cudaMemsetAsync(ctx->pp.err, 0, sizeof(int32_t), ctx->stream);
-        return fail(ctx, TB_ERR_CUDA, "persistent Chebyshev kernel: neighbour wait timed out");
-    }
-    return TB_OK;
+    return check_kernel_flags(ctx);
 }
 
 int state_status(tb_ctx *ctx, const DevState &hs)
@@ -664,6 +830,7 @@ void fill_report(tb_ctx *ctx, cudaEvent_t e0, const DevState &hs, int iters, tb_
     rep->scc_iters = iters;
     rep->bisect_rounds = hs.bisect_rounds;
     rep->column_block = ctx->w.B;
+    rep->step_kernel = ctx->w.precision == TB_PREC_FP32 ? ctx->w.kind : 0;
     rep->precision = ctx->p.precision;
     rep->t_total_ms = tot;
     rep->t_moments_ms = tm;
@@ -721,6 +888,11 @@ void free_all(tb_ctx *ctx)
     dfree(ctx->sp.lcol);
     dfree(ctx->sp.lself);
     ctx->sp = StagePlan{};
+    dfree(ctx->pl.hdr);
+    dfree(ctx->pl.runs);
+    dfree(ctx->pl.rec);
+    dfree(ctx->pl.err);
+    ctx->pl = PipePlan{};
     dfree(ctx->pp.lcode);
     dfree(ctx->pp.hptr);
     dfree(ctx->pp.hrows);
@@ -997,7 +1169,7 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
     TB_TRY(set_device(ctx));
     free_all(ctx);
     ctx->have_h = ctx->have_scc = false;
-    ctx->tuned[0] = ctx->tuned[1] = 0;
+    reset_tuning(ctx);
     DevMatrix &m = ctx->m;
     m.n = n;
     m.natoms = natoms;
@@ -1013,6 +1185,7 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
     TB_TRY(dalloc(ctx, m.xdiag32, (size_t)n));
     TB_TRY(build_stage_plan(ctx, hb.brow, hb.bcol));
     TB_TRY(build_persist_plan(ctx, hb.brow, hb.bcol));
+    TB_TRY(build_pipe_plan(ctx, hb.brow, hb.bcol));
     ctx->h0_lmin = hb.lmin;
     ctx->h0_lmax = hb.lmax;
     TB_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1041,7 +1214,7 @@ int tb_set_geometry(tb_ctx *ctx, int32_t natoms, const double *xyz, const int32_
     TB_TRY(set_device(ctx));
     free_all(ctx);
     ctx->have_h = ctx->have_scc = false;
-    ctx->tuned[0] = ctx->tuned[1] = 0;
+    reset_tuning(ctx);
     GeomDevice g;
     const int rc = geom_build_device(ctx->stream, natoms, xyz, species, box, rcut_bohr, gamma_diag, g, ctx->err);
     DevMatrix &m = ctx->m;
@@ -1072,6 +1245,7 @@ int tb_set_geometry(tb_ctx *ctx, int32_t natoms, const double *xyz, const int32_
     TB_TRY(dalloc(ctx, sc.hist_meta, 2));
     TB_TRY(build_stage_plan(ctx, g.brow, g.bcol));
     TB_TRY(build_persist_plan(ctx, g.brow, g.bcol));
+    TB_TRY(build_pipe_plan(ctx, g.brow, g.bcol));
     double mn = 1e300, mx = -1e300, ne = 0.0;
     for (int i = 0; i < m.n; i++) {
         mn = std::min(mn, g.h0diag_h[i] - g.radius_h[i]);

@@ -60,6 +60,23 @@ struct StagePlan {
     int32_t *lself = nullptr;     // nb: local index of block row I in its own group's list
 };
 
+// Plan of the pipelined FP32 kernel (k_cheb_f32_pipe): row groups of R block
+// rows; per group a header {nu, tb0, nbk, rec_off, rec_len, run_off, nruns,
+// nr}, the runs of consecutive distinct referenced rows {J0, rows, slot0, 0}
+// and a packed index record [local row offsets (nr+1) | local column per
+// block (nbk) | own-row slot (nr)] padded to 4 ints (16-byte aligned).
+struct PipePlan {
+    int32_t R = 0, G = 0, maxU = 0, maxBlk = 0, stages = 0, nsm = 0;
+    size_t stage_bytes = 0;
+    int32_t *hdr = nullptr;
+    int32_t *runs = nullptr;
+    int32_t *rec = nullptr;
+    int32_t *err = nullptr;  // device error flag (bounded waits)
+};
+
+// Chebyshev step kernels of the FP32 form (values of tb_params.fp32_kernel).
+enum StepKind { kKindAuto = 0, kKindStaged = 1, kKindPersistent = 2, kKindPipelined = 3 };
+
 // Task plan of the persistent FP32 kernel (see k_cheb_f32_persistent).
 struct PersistPlan {
     int32_t R = 0, G = 0, nc = 0, B = 0, maxH = 0, maxBlk = 0, maxNG = 0;
@@ -88,7 +105,7 @@ struct DevWork {
     int32_t M = 0, nq_cap = 0, B = 0, K = 0, rowgroups = 0;
     int32_t precision = -1;
     int32_t kernel = -1;
-    bool persist = false;       // FP32 form through k_cheb_f32_persistent
+    int32_t kind = 0;           // StepKind of the FP32 form (kKindStaged for FP64)
     double *shift = nullptr;   // n
     double *d = nullptr;       // (M+1) * n diagonal moments [k][i]
     double *mom = nullptr;     // M+1
@@ -120,13 +137,17 @@ struct tb_ctx {
     tb::DevWork w;
     tb::StagePlan sp;
     tb::PersistPlan pp;
+    tb::PipePlan pl;
     int64_t launches = 0;
     int64_t spmm_launches = 0;
     double spmm_bytes = 0.0;
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> moment_events;
     size_t ev_used = 0;
-    int tuned[2] = {0, 0};  // per precision: 0 untuned, -1 persistent, else slab width
+    // autotuner result per precision and requested fp32_kernel: kind and slab
+    // width (0 = not tuned yet)
+    int tuned_kind[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    int tuned_B[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     // SP2 device scratch (lazily sized)
     void *sp2_scratch = nullptr;
     size_t sp2_scratch_bytes = 0;
@@ -157,6 +178,17 @@ int cheb_f32_persistent_setup(int R, size_t smem, int *ctas_per_sm);  // returns
 int launch_cheb_f32_persistent(cudaStream_t st, const DevMatrix &m, const PersistPlan &pp, int K,
                                int B, int c0, float *G0, float *G1, double *partial, int *flags,
                                int *err);  // returns a cudaError_t
+// ---- tb_pipe.cu ----
+size_t cheb_f32_pipe_stage_bytes(int R, int maxU, int maxBlk, int rec_cap);
+// identity columns in the chunk-major slab layout [B/64][n][64] of the pipelined kernel
+void launch_slab_identity_cm(cudaStream_t st, float *T0, int n, int B, int c0);
+size_t cheb_f32_pipe_smem(size_t stage_bytes, int stages);
+int cheb_f32_pipe_configure(size_t smem);  // returns a cudaError_t
+// partial_k: float2 (hi, lo) pairs in the slots of the double partial array
+int launch_cheb_step_f32_pipe(cudaStream_t st, const DevMatrix &m, const PipePlan &pl, const float *Tin,
+                              float *Tout, int B, int first, float2 *partial_k);
+void launch_f32_finalize_pairs(cudaStream_t st, const DevMatrix &m, const float2 *partial, int K, int rowgroups,
+                               int B, int c0, double *d, int M);
 int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const StagePlan &sp,
                                 const float *Tin, float *Tout, int B, int first,
                                 double *partial_k);

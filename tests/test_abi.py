@@ -59,6 +59,8 @@ def test_bad_params_rejected_before_device():
     assert L.tb_ctx_create(C.byref(p), C.byref(h)) == T.api.TB_ERR_INVALID_ARG
     p = T.params(column_block=100)
     assert L.tb_ctx_create(C.byref(p), C.byref(h)) == T.api.TB_ERR_INVALID_ARG
+    p = T.params(fp32_kernel=4)
+    assert L.tb_ctx_create(C.byref(p), C.byref(h)) == T.api.TB_ERR_INVALID_ARG
     p = T.params()
     p.struct_size = 8
     assert L.tb_ctx_create(C.byref(p), C.byref(h)) == T.api.TB_ERR_INVALID_ARG

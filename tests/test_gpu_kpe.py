@@ -237,3 +237,45 @@ def test_full_size_fp32_vs_fp64_properties(gpu):
     # mu_0 = tr I = n exactly; tr X equals the scaled trace of H
     assert abs(out[0]["moments"][0] - m.n) < 1e-9
     assert np.all(out[0]["diagP"] > -1e-6) and np.all(out[0]["diagP"] < 1 + 1e-6)
+
+
+@pytest.mark.parametrize("kern", [1, 2, 3])
+@pytest.mark.parametrize("dims,B", [((2, 2, 2), 0), ((1, 2, 3), 0), ((2, 2, 2), 128), ((1, 1, 3), 256)])
+def test_fp32_step_kernels_match_oracle(gpu, kern, dims, B):
+    """Each FP32 step kernel (staged, persistent, pipelined), forced, with the
+    autotuned and with fixed slab widths, against the FP64 oracle."""
+    m, o = _pair(*dims, seed=23)
+    ref = O.density(o, O.kpe_params(M=160, kT=0.01, n_elec=o.n_elec))
+    with _ctx(gpu, m, M=160, precision=gpu.PREC_FP32, fp32_kernel=kern, column_block=B) as c:
+        r = c.density()
+    rep = r["report"]
+    assert rep["step_kernel"] == kern
+    if kern != 2 and B:
+        assert rep["column_block"] == min(B, -(-m.n // 64) * 64)
+    assert np.abs(r["q"] - ref["q"]).max() < 1e-6
+    assert abs(r["e_band"] - ref["e_band"]) / m.natoms < 1e-7
+    assert abs(r["q"].sum() - m.n_electrons) < 1e-6
+
+
+def test_pipelined_equals_staged_recurrence(gpu):
+    """The pipelined and staged kernels run the same FP32 multiply-add chain
+    per block row; only the FP64 order of the row partials differs, so the
+    charges agree far below the FP32 tolerance."""
+    import largetb_gb300 as T
+    m = T.model_cristobalite(3, 3, 3, sigma_ang=0.08, seed=31)
+    out = {}
+    for kern in (1, 3):
+        with _ctx(gpu, m, M=300, precision=gpu.PREC_FP32, fp32_kernel=kern, column_block=512) as c:
+            out[kern] = c.density()
+    assert np.abs(out[1]["q"] - out[3]["q"]).max() < 1e-10
+    np.testing.assert_allclose(out[1]["moments"], out[3]["moments"], rtol=0, atol=1e-9 * m.n)
+
+
+def test_autotuner_reports_a_kernel(gpu):
+    import largetb_gb300 as T
+    m = T.model_cristobalite(2, 2, 3, sigma_ang=0.05, seed=5)
+    with _ctx(gpu, m, M=60, precision=gpu.PREC_FP32) as c:
+        rep = c.density()["report"]
+        again = c.density()["report"]
+    assert rep["step_kernel"] in (1, 2, 3)
+    assert (again["step_kernel"], again["column_block"]) == (rep["step_kernel"], rep["column_block"])
