@@ -66,6 +66,9 @@ def allmax(ws, x):
     return float(t.item())
 
 
+STEP_KERNELS = {1: "k_cheb_f32_staged", 2: "k_cheb_f32_persistent", 3: "k_cheb_f32_pipe", 4: "k_cheb_f32_pipe"}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -323,7 +326,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--column-block", type=int, default=0)
     ap.add_argument("--fp32-kernel", type=int, default=0,
-                    help="0 autotune, 1 staged, 2 persistent, 3 pipelined")
+                    help="0 autotune, 1 staged, 2 persistent, 3 pipelined (one launch per slab), "
+                         "4 pipelined (one launch per step)")
     ap.add_argument("--density-only", action="store_true",
                     help="time single density evaluations (the unit profiled with ncu)")
     ap.add_argument("--zero-start", action="store_true",
@@ -468,7 +472,7 @@ def main():
         "wall_s_per_step": wall / args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_source": src,
-                     "kernel": "k_cheb_f32", "launches": int(spmm_l),
+                     "kernel": STEP_KERNELS.get(rep["step_kernel"], "k_cheb_f32"), "launches": int(spmm_l),
                      "avg_launch_us": sum(mom_ms) * 1e3 / max(1, spmm_l),
                      "bytes_per_launch": spmm_b / max(1, spmm_l)},
         "clocks": clk,
@@ -486,6 +490,11 @@ def main():
                               "speedup_fast_vs_plain": rep64["t_total_ms"] / 1e3 / value,
                               "max_dq_fast_vs_plain": float(np.abs(q32 - r64["q"]).max()),
                               "e_band_diff_per_atom": abs(eb32 - r64["e_band"]) / m.natoms}
+        # FP32 error alone: both forms on the same H (H0 + Gamma shift of the FP32 charges)
+        shift = ctx.coulomb_shift(q32)[m.orb2atom]
+        d32, d64 = ctx.density(shift), ctx64.density(shift)
+        line["plain_fp64"]["same_H"] = {"max_dq": float(np.abs(d32["q"] - d64["q"]).max()),
+                                        "e_band_diff_per_atom": abs(d32["e_band"] - d64["e_band"]) / m.natoms}
         ctx64.close()
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O

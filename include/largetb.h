@@ -65,7 +65,9 @@ enum tb_fp32_kernel {
                                with column_block set: pipelined where it fits, else staged */
     TB_FP32_STAGED = 1,     /* one launch per step, row-group staging in shared memory */
     TB_FP32_PERSISTENT = 2, /* one cooperative launch per slab, neighbour-synchronised */
-    TB_FP32_PIPELINED = 3   /* one launch per step, SM-resident CTAs with a bulk-copy stage ring */
+    TB_FP32_PIPELINED = 3,     /* SM-resident CTAs with a bulk-copy stage ring; one cooperative
+                                  launch per slab, tiles synchronised with their neighbours */
+    TB_FP32_PIPELINED_STEP = 4 /* the same kernel, one launch per step */
 };
 
 enum tb_kernel_kind {

@@ -44,6 +44,7 @@ FP32_AUTO = 0
 FP32_STAGED = 1
 FP32_PERSISTENT = 2
 FP32_PIPELINED = 3
+FP32_PIPELINED_STEP = 4
 
 
 class TbParams(C.Structure):

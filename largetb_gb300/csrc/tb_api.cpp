@@ -124,7 +124,7 @@ int check_params(tb_ctx *ctx, const tb_params *p)
         return fail(ctx, TB_ERR_INVALID_ARG, "bad pad / tolerance / iteration cap");
     if (p->mix_history < 0 || p->mix_history > kMaxHistory || !(p->mix_beta > 0))
         return fail(ctx, TB_ERR_INVALID_ARG, "mix_history must be in [0,16], mix_beta > 0");
-    if (p->fp32_kernel < TB_FP32_AUTO || p->fp32_kernel > TB_FP32_PIPELINED)
+    if (p->fp32_kernel < TB_FP32_AUTO || p->fp32_kernel > TB_FP32_PIPELINED_STEP)
         return fail(ctx, TB_ERR_INVALID_ARG, "unknown fp32_kernel");
     if (!(p->sp2_drop_tol >= 0) || p->sp2_max_iter < 1 || !(p->sp2_idem_tol >= 0))
         return fail(ctx, TB_ERR_INVALID_ARG, "bad SP2 parameters");
@@ -142,7 +142,7 @@ double step_bytes(const DevMatrix &m, int B, int s);
 void reset_tuning(tb_ctx *ctx)
 {
     for (int a = 0; a < 2; a++)
-        for (int b = 0; b < 4; b++) ctx->tuned_kind[a][b] = ctx->tuned_B[a][b] = 0;
+        for (int b = 0; b < kNumKinds; b++) ctx->tuned_kind[a][b] = ctx->tuned_B[a][b] = 0;
 }
 
 // Error flags raised by the bounded waits of the persistent and pipelined
@@ -163,6 +163,20 @@ int check_kernel_flags(tb_ctx *ctx)
         cudaMemsetAsync(ctx->pl.err, 0, sizeof(int32_t), ctx->stream);
         return fail(ctx, TB_ERR_CUDA, "pipelined Chebyshev kernel: stage wait timed out");
     }
+    return TB_OK;
+}
+
+// Step-flag array of the one-launch-per-slab pipelined mode: one int per
+// tile (row group x 64-column chunk) of a B-column slab.
+int ensure_pipe_flags(tb_ctx *ctx, int B)
+{
+    PipePlan &pl = ctx->pl;
+    const int64_t need = (int64_t)pl.G * ((B + 63) / 64);
+    if (pl.flags && pl.flags_cap >= need) return TB_OK;
+    dfree(pl.flags);
+    pl.flags_cap = 0;
+    TB_TRY(dalloc(ctx, pl.flags, (size_t)need));
+    pl.flags_cap = need;
     return TB_OK;
 }
 
@@ -194,8 +208,10 @@ int autotune(tb_ctx *ctx, int req)
     };
     if (prec == TB_PREC_FP32) {
         if ((req == kKindAuto || req == kKindPersistent) && ctx->pp.R > 0) cands.push_back({kKindPersistent, ctx->pp.B});
-        if ((req == kKindAuto || req == kKindPipelined) && ctx->pl.stages > 0)
+        if ((req == kKindAuto || req == kKindPipelined) && ctx->pl.stages > 0 && ctx->pl.coop)
             widths(kKindPipelined, {256, 512, 1024}, 64);
+        if ((req == kKindAuto || req == kKindPipelinedStep) && ctx->pl.stages > 0)
+            widths(kKindPipelinedStep, {512, 1024}, 64);
         if (req == kKindAuto || req == kKindStaged) widths(kKindStaged, {256, 384, 512}, ctx->sp.R > 0 ? 64 : 128);
     } else {
         widths(kKindStaged, {64, 128, 256}, 64);
@@ -215,9 +231,11 @@ int autotune(tb_ctx *ctx, int req)
     for (const Cand &cd : cands) {
         const int B = cd.B;
         const size_t es = prec == TB_PREC_FP32 ? 4 : 8;
-        const int rowgroups = cd.kind == kKindPersistent   ? ctx->pp.G
-                              : cd.kind == kKindPipelined ? ctx->pl.G
-                                                          : (ctx->sp.R > 0 ? ctx->sp.G : cheb_f32_rowgroups(m.nb));
+        const bool pipe = cd.kind == kKindPipelined || cd.kind == kKindPipelinedStep;
+        const int rowgroups = cd.kind == kKindPersistent ? ctx->pp.G
+                              : pipe                     ? ctx->pl.G
+                                                         : (ctx->sp.R > 0 ? ctx->sp.G : cheb_f32_rowgroups(m.nb));
+        if (cd.kind == kKindPipelined) TB_TRY(ensure_pipe_flags(ctx, B));
         char *T0 = nullptr, *T1 = nullptr;
         double *part = nullptr, *dd = nullptr;
         TB_TRY(dalloc(ctx, T0, (size_t)m.n * B * es));
@@ -233,8 +251,15 @@ int autotune(tb_ctx *ctx, int req)
                 cudaMemsetAsync(ctx->pp.flags, 0, sizeof(int32_t) * ctx->pp.G * ctx->pp.nc, st);
                 launch_cheb_f32_persistent(st, m, ctx->pp, kTuneSteps, B, 0, (float *)T0, (float *)T1, part,
                                            ctx->pp.flags, ctx->pp.err);
+            } else if (cd.kind == kKindPipelined) {
+                launch_slab_identity_cm(st, (float *)T0, m.n, B, 0);
+                const int e = launch_cheb_f32_pipe(st, m, ctx->pl, (float *)T0, (float *)T1, B, 0, kTuneSteps,
+                                                   reinterpret_cast<float2 *>(part), true);
+                if (e != (int)cudaSuccess)
+                    return fail(ctx, TB_ERR_CUDA,
+                                std::string("cooperative launch: ") + cudaGetErrorString((cudaError_t)e));
             } else {
-                if (cd.kind == kKindPipelined)
+                if (cd.kind == kKindPipelinedStep)
                     launch_slab_identity_cm(st, (float *)T0, m.n, B, 0);
                 else
                     launch_slab_identity(st, T0, m.n, B, 0, prec);
@@ -244,9 +269,9 @@ int autotune(tb_ctx *ctx, int req)
                     double *pk = part ? part + (int64_t)k * rowgroups * B * 2 : nullptr;
                     if (prec == TB_PREC_FP64)
                         launch_cheb_step_f64(st, m, (double *)in, (double *)out, B, 0, k == 0, dd, k + 1);
-                    else if (cd.kind == kKindPipelined)
-                        launch_cheb_step_f32_pipe(st, m, ctx->pl, (float *)in, (float *)out, B, k == 0,
-                                                  reinterpret_cast<float2 *>(pk));
+                    else if (cd.kind == kKindPipelinedStep)
+                        launch_cheb_f32_pipe(st, m, ctx->pl, (float *)T0, (float *)T1, B, k, 1,
+                                             reinterpret_cast<float2 *>(pk), false);
                     else if (ctx->sp.R > 0)
                         launch_cheb_step_f32_staged(st, m, ctx->sp, (float *)in, (float *)out, B, k == 0, pk);
                     else
@@ -292,12 +317,15 @@ int ensure_work(tb_ctx *ctx)
         kind = ctx->tuned_kind[prec][req];
         B = ctx->tuned_B[prec][req];
     } else if (prec == TB_PREC_FP32) {
-        kind = req != kKindAuto ? req : (ctx->pl.stages > 0 ? kKindPipelined : kKindStaged);
+        kind = req != kKindAuto ? req
+                                : (ctx->pl.stages > 0 ? (ctx->pl.coop ? kKindPipelined : kKindPipelinedStep) : kKindStaged);
     }
     if (kind == kKindPersistent && ctx->pp.R == 0)
         return fail(ctx, TB_ERR_UNSUPPORTED, "persistent FP32 kernel: no task plan fits this matrix");
-    if (kind == kKindPipelined && ctx->pl.stages == 0)
+    if ((kind == kKindPipelined || kind == kKindPipelinedStep) && ctx->pl.stages == 0)
         return fail(ctx, TB_ERR_UNSUPPORTED, "pipelined FP32 kernel: no stage plan fits this matrix");
+    if (kind == kKindPipelined && !ctx->pl.coop)
+        return fail(ctx, TB_ERR_UNSUPPORTED, "pipelined FP32 kernel: cooperative launch not available");
     if (kind == kKindPersistent) {
         B = ctx->pp.B;
     } else {
@@ -307,10 +335,12 @@ int ensure_work(tb_ctx *ctx)
         if (B > nround) B = nround;
     }
     const bool persist = kind == kKindPersistent;
+    const bool pipe = kind == kKindPipelined || kind == kKindPipelinedStep;
+    if (kind == kKindPipelined) TB_TRY(ensure_pipe_flags(ctx, B));
     const int K = (prec == TB_PREC_FP32) ? (M + 2) / 2 : 0;
     const int rowgroups = (prec != TB_PREC_FP32)       ? 0
                           : persist                      ? ctx->pp.G
-                          : kind == kKindPipelined       ? ctx->pl.G
+                          : pipe                         ? ctx->pl.G
                           : ctx->sp.R > 0                ? ctx->sp.G
                                                          : cheb_f32_rowgroups(m.nb);
     w.kind = kind;
@@ -471,6 +501,9 @@ int build_pipe_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::ve
     dfree(pl.hdr);
     dfree(pl.runs);
     dfree(pl.rec);
+    dfree(pl.nbr_ptr);
+    dfree(pl.nbr);
+    dfree(pl.flags);
     dfree(pl.err);
     pl = PipePlan{};
     const int nb = (int)brow.size() - 1;
@@ -505,20 +538,25 @@ int build_pipe_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::ve
         if (stages < 2) continue;
         const int64_t tiles = (int64_t)G * 8;
         const double eff = (double)tiles / (double)(((tiles + nsm - 1) / nsm) * nsm);
-        const double cost = (double)(tot + nb) / eff * (stages == 3 ? 1.0 : 1.25);
+        const double cost = (double)(tot + nb) / eff * (stages >= 3 ? 1.0 : 1.25);
         if (cost < best.cost) best = {R, stages, cost};
     }
     if (best.R == 0) return TB_OK;  // pipelined kernel unavailable for this matrix
     const int R = best.R, G = (nb + R - 1) / R;
-    std::vector<int32_t> hdr((size_t)G * 8, 0), runs, rec;
-    int maxU = 0, maxBlk = 0, rec_cap = 0;
+    std::vector<int32_t> hdr((size_t)G * 8, 0), rec, nptr(G + 1, 0), nbr;
+    std::vector<std::vector<int32_t>> grun(G);
+    int maxU = 0, maxBlk = 0, rec_cap = 0, maxRuns = 0;
     for (int g = 0; g < G; g++) {
         const int I0 = g * R, I1 = std::min(nb, I0 + R), tb0 = brow[I0];
         std::vector<int32_t> U(bcol.begin() + tb0, bcol.begin() + brow[I1]);
         std::sort(U.begin(), U.end());
         U.erase(std::unique(U.begin(), U.end()), U.end());
         const int nu = (int)U.size();
-        const size_t rstart = rec.size(), run0 = runs.size() / 4;
+        const size_t rstart = rec.size();
+        std::vector<int32_t> &runs = grun[g];
+        for (int J : U)  // U is sorted, so the owner groups come in order
+            if (nbr.size() == (size_t)nptr[g] || nbr.back() != J / R) nbr.push_back(J / R);
+        nptr[g + 1] = (int32_t)nbr.size();
         for (int I = I0; I <= I1; I++) rec.push_back(brow[I] - tb0);
         for (int t = tb0; t < brow[I1]; t++)
             rec.push_back((int32_t)(std::lower_bound(U.begin(), U.end(), bcol[t]) - U.begin()));
@@ -536,8 +574,9 @@ int build_pipe_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::ve
         h[2] = brow[I1] - tb0;
         h[3] = (int32_t)rstart;
         h[4] = (int32_t)(rec.size() - rstart);
-        h[5] = (int32_t)run0;
-        h[6] = (int32_t)(runs.size() / 4 - run0);
+        h[5] = 0;
+        h[6] = (int32_t)(runs.size() / 4);
+        maxRuns = std::max(maxRuns, h[6]);
         h[7] = I1 - I0;
         maxU = std::max(maxU, nu);
         maxBlk = std::max(maxBlk, h[2]);
@@ -545,11 +584,19 @@ int build_pipe_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::ve
     }
     const size_t stage_bytes = cheb_f32_pipe_stage_bytes(R, maxU, maxBlk, rec_cap);
     const size_t smem = cheb_f32_pipe_smem(stage_bytes, best.stages);
-    if (smem > 227 * 1024 || cheb_f32_pipe_configure(smem) != (int)cudaSuccess) {
+    int per_sm = 0;
+    if (smem > 227 * 1024 || cheb_f32_pipe_configure(smem, &per_sm) != (int)cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         return TB_OK;
     }
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+    const int run_stride = (maxRuns + 31) / 32 * 32;
+    std::vector<int32_t> runs((size_t)G * run_stride * 4, 0);
+    for (int g = 0; g < G; g++) std::copy(grun[g].begin(), grun[g].end(), runs.begin() + (size_t)g * run_stride * 4);
     TB_TRY(upload(ctx, pl.hdr, hdr.data(), hdr.size()));
+    TB_TRY(upload(ctx, pl.nbr_ptr, nptr.data(), nptr.size()));
+    TB_TRY(upload(ctx, pl.nbr, nbr.data(), nbr.size()));
     TB_TRY(upload(ctx, pl.runs, runs.data(), runs.size()));
     TB_TRY(upload(ctx, pl.rec, rec.data(), rec.size()));
     TB_TRY(dalloc(ctx, pl.err, 1));
@@ -561,6 +608,8 @@ int build_pipe_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::ve
     pl.stages = best.stages;
     pl.stage_bytes = stage_bytes;
     pl.nsm = nsm;
+    pl.run_stride = run_stride;
+    pl.coop = coop != 0;
     return TB_OK;
 }
 
@@ -701,7 +750,7 @@ int density_eval(tb_ctx *ctx, bool have_shift)
     const int nslab = (m.n + B - 1) / B;
     for (int s = 0; s < nslab; s++) {
         const int c0 = s * B;
-        if (w.kind == kKindPipelined) {
+        if (w.kind == kKindPipelined || w.kind == kKindPipelinedStep) {
             launch_slab_identity_cm(st, (float *)w.T0, m.n, B, c0);
             ctx->launches++;
         } else if (w.kind != kKindPersistent) {
@@ -717,6 +766,17 @@ int density_eval(tb_ctx *ctx, bool have_shift)
             }
             ctx->spmm_launches += M;
             ctx->spmm_bytes += M * step_bytes(m, B, 8);
+        } else if (w.kind == kKindPipelined) {
+            const int e = launch_cheb_f32_pipe(st, m, ctx->pl, (float *)w.T0, (float *)w.T1, B, 0, w.K,
+                                               reinterpret_cast<float2 *>(w.partial), true);
+            if (e != (int)cudaSuccess)
+                return fail(ctx, TB_ERR_CUDA,
+                            std::string("cooperative launch: ") + cudaGetErrorString((cudaError_t)e));
+            launch_f32_finalize_pairs(st, m, reinterpret_cast<const float2 *>(w.partial), w.K, w.rowgroups, B, c0,
+                                      w.d, M);
+            ctx->launches += 3;  // flag reset, slab kernel, finalize
+            ctx->spmm_launches += w.K;  // one launch carries all K slab steps
+            ctx->spmm_bytes += w.K * step_bytes(m, B, 4);
         } else if (w.kind == kKindPersistent) {
             TB_CUDA(cudaMemsetAsync(ctx->pp.flags, 0, sizeof(int32_t) * ctx->pp.G * ctx->pp.nc, st));
             const int e = launch_cheb_f32_persistent(st, m, ctx->pp, w.K, B, c0, (float *)w.T0,
@@ -735,16 +795,15 @@ int density_eval(tb_ctx *ctx, bool have_shift)
                 const int kout = k + 1;
                 const bool odd = kout & 1;
                 double *pk = w.partial + (int64_t)k * w.rowgroups * B * 2;
-                if (w.kind == kKindPipelined)
-                    launch_cheb_step_f32_pipe(st, m, ctx->pl, odd ? A : Bf, odd ? Bf : A, B, k == 0,
-                                              reinterpret_cast<float2 *>(pk));
+                if (w.kind == kKindPipelinedStep)
+                    launch_cheb_f32_pipe(st, m, ctx->pl, A, Bf, B, k, 1, reinterpret_cast<float2 *>(pk), false);
                 else if (ctx->sp.R > 0)
                     launch_cheb_step_f32_staged(st, m, ctx->sp, odd ? A : Bf, odd ? Bf : A, B, k == 0, pk);
                 else
                     launch_cheb_step_f32(st, m, odd ? A : Bf, odd ? Bf : A, B, k == 0, pk, w.rowgroups);
                 ctx->launches++;
             }
-            if (w.kind == kKindPipelined)
+            if (w.kind == kKindPipelinedStep)
                 launch_f32_finalize_pairs(st, m, reinterpret_cast<const float2 *>(w.partial), w.K, w.rowgroups, B,
                                           c0, w.d, M);
             else
@@ -891,6 +950,9 @@ void free_all(tb_ctx *ctx)
     dfree(ctx->pl.hdr);
     dfree(ctx->pl.runs);
     dfree(ctx->pl.rec);
+    dfree(ctx->pl.nbr_ptr);
+    dfree(ctx->pl.nbr);
+    dfree(ctx->pl.flags);
     dfree(ctx->pl.err);
     ctx->pl = PipePlan{};
     dfree(ctx->pp.lcode);

@@ -61,21 +61,34 @@ struct StagePlan {
 };
 
 // Plan of the pipelined FP32 kernel (k_cheb_f32_pipe): row groups of R block
-// rows; per group a header {nu, tb0, nbk, rec_off, rec_len, run_off, nruns,
-// nr}, the runs of consecutive distinct referenced rows {J0, rows, slot0, 0}
-// and a packed index record [local row offsets (nr+1) | local column per
+// rows; per group a header {nu, tb0, nbk, rec_off, rec_len, 0, nruns, nr},
+// the runs of consecutive distinct referenced rows {J0, rows, slot0, 0} at a
+// fixed stride of run_stride per group, and a packed index record [local row offsets (nr+1) | local column per
 // block (nbk) | own-row slot (nr)] padded to 4 ints (16-byte aligned).
 struct PipePlan {
     int32_t R = 0, G = 0, maxU = 0, maxBlk = 0, stages = 0, nsm = 0;
+    int32_t run_stride = 0;  // runs per group slot (a multiple of 32)
+    bool coop = false;       // one CTA per SM fits: the one-launch-per-slab mode is available
     size_t stage_bytes = 0;
     int32_t *hdr = nullptr;
     int32_t *runs = nullptr;
     int32_t *rec = nullptr;
+    int32_t *nbr_ptr = nullptr;  // G+1
+    int32_t *nbr = nullptr;      // groups owning rows that group g references (g included)
+    int32_t *flags = nullptr;    // completed steps per tile of the one-launch-per-slab mode
+    int64_t flags_cap = 0;
     int32_t *err = nullptr;  // device error flag (bounded waits)
 };
 
 // Chebyshev step kernels of the FP32 form (values of tb_params.fp32_kernel).
-enum StepKind { kKindAuto = 0, kKindStaged = 1, kKindPersistent = 2, kKindPipelined = 3 };
+enum StepKind {
+    kKindAuto = 0,
+    kKindStaged = 1,
+    kKindPersistent = 2,
+    kKindPipelined = 3,     // k_cheb_f32_pipe, one cooperative launch per slab
+    kKindPipelinedStep = 4  // k_cheb_f32_pipe, one launch per step
+};
+constexpr int kNumKinds = 5;
 
 // Task plan of the persistent FP32 kernel (see k_cheb_f32_persistent).
 struct PersistPlan {
@@ -146,8 +159,8 @@ struct tb_ctx {
     size_t ev_used = 0;
     // autotuner result per precision and requested fp32_kernel: kind and slab
     // width (0 = not tuned yet)
-    int tuned_kind[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
-    int tuned_B[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    int tuned_kind[2][tb::kNumKinds] = {};
+    int tuned_B[2][tb::kNumKinds] = {};
     // SP2 device scratch (lazily sized)
     void *sp2_scratch = nullptr;
     size_t sp2_scratch_bytes = 0;
@@ -183,10 +196,14 @@ size_t cheb_f32_pipe_stage_bytes(int R, int maxU, int maxBlk, int rec_cap);
 // identity columns in the chunk-major slab layout [B/64][n][64] of the pipelined kernel
 void launch_slab_identity_cm(cudaStream_t st, float *T0, int n, int B, int c0);
 size_t cheb_f32_pipe_smem(size_t stage_bytes, int stages);
-int cheb_f32_pipe_configure(size_t smem);  // returns a cudaError_t
-// partial_k: float2 (hi, lo) pairs in the slots of the double partial array
-int launch_cheb_step_f32_pipe(cudaStream_t st, const DevMatrix &m, const PipePlan &pl, const float *Tin,
-                              float *Tout, int B, int first, float2 *partial_k);
+int cheb_f32_pipe_configure(size_t smem, int *ctas_per_sm);  // returns a cudaError_t
+// Steps k0 .. k0+steps-1 of a slab held in T0/T1 (chunk-major; step k reads
+// T_k from T0 when k is even); partial: float2 (hi, lo) pairs in the slots of
+// the double partial array, block k - k0 per step.  multi: one cooperative
+// launch synchronised by per-tile flags; else a plain launch (steps = 1).
+// Returns a cudaError_t.
+int launch_cheb_f32_pipe(cudaStream_t st, const DevMatrix &m, const PipePlan &pl, float *T0, float *T1, int B,
+                         int k0, int steps, float2 *partial, bool multi);
 void launch_f32_finalize_pairs(cudaStream_t st, const DevMatrix &m, const float2 *partial, int K, int rowgroups,
                                int B, int c0, double *d, int M);
 int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const StagePlan &sp,

@@ -1,6 +1,6 @@
-// tb_pipe.cu -- FP32 Chebyshev step, pipelined form (K2 of the density-matrix
-// path: the recurrence of getKPE, withSP2_deltaH.cpp:1134-1168, over identity
-// columns, with the moments taken from column dot products as in
+// tb_pipe.cu -- FP32 Chebyshev recurrence, pipelined form (K2 of the
+// density-matrix path: the recurrence of getKPE, withSP2_deltaH.cpp:1134-1168,
+// over identity columns, with the moments taken from column dot products as in
 // k_cheb_f32_staged).
 //
 // Slab layout: chunk-major, [B/64][n][64] floats, so that a block row of one
@@ -13,9 +13,23 @@
 // completion counted in bytes on the stage's "full" mbarrier): the group's
 // distinct referenced block rows of T_k as runs of consecutive rows (one copy
 // per run), its own rows of T_{k-1} (one copy), its X blocks (one copy) and a
-// packed index record (one copy).  Eight consumer warps compute the tile from
-// shared memory while the producer fills the next stages.  Tile headers are
-// read one tile ahead, so the producer never waits on its own index loads.
+// packed index record (one copy).  Twelve consumer warps compute the tile from
+// shared memory while the producer fills the next stages.  The header and
+// copy runs of the next tile are loaded while the producer waits for a free
+// stage, so no global load latency sits on its path.
+//
+// Two launch modes share the kernel:
+//  - one launch per step (steps = 1);
+//  - one cooperative launch per slab running all K steps.  A tile publishes
+//    its step count in flags[tile] (release, after a CTA barrier over its
+//    stores); before the producer copies tile (chunk, g) of step k >= 1 it
+//    waits (acquire) until every group g' whose rows g references, g itself
+//    included, has published step k in the same chunk.  That covers both the
+//    T_k rows it reads and the T_{k-1} rows it overwrites: the block pattern is
+//    symmetric, so the groups that read rows of g at step k-1 are exactly those
+//    neighbours.  Each CTA runs its tiles in step order and all CTAs are
+//    co-resident, so the oldest unfinished step can always proceed.  The
+//    pipeline never drains between steps.
 //
 // Column dot products <T_k,T_k> and <T_k,T_{k+1}> accumulate in FP32 over one
 // block row and then as unevaluated FP32 pairs (hi, lo) across rows and warps:
@@ -24,14 +38,16 @@
 // about 2 operations per clock per SM, so per-row FP64 accumulation would cost
 // as much as the rest of the step; the pairs keep ~44 significant bits with
 // FP32 arithmetic only.  The consumer warps' pairs are summed in a fixed order
-// through a double-buffered shared array (one named barrier per tile), giving
-// partial[g][col][2] as float2 (hi, lo); k_f32_finalize_pairs converts to FP64.
+// through a shared array (two named barriers per tile), giving
+// partial[k][g][col][2] as float2 (hi, lo); k_f32_finalize_pairs converts to
+// FP64.
 //
-// Every mbarrier wait is bounded: after kPipeSpin unsuccessful polls the
-// thread raises a block-wide abort flag and the device error flag; all
-// consumer warps still run the same tile sequence (so the named barriers stay
-// matched) but skip the work, and the producer, before it returns, waits (again
-// bounded) for the copies it has issued.
+// Every wait is bounded: after kPipeSpin unsuccessful polls the thread raises
+// a block-wide abort flag and the device error flag; all consumer warps still
+// run the same tile sequence (so the named barriers stay matched) but skip the
+// work, other CTAs waiting on this one's flags time out the same way, and the
+// producer, before it returns, waits (again bounded) for the copies it has
+// issued.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,18 +59,23 @@ namespace tb {
 namespace {
 
 constexpr int kPipeCols = 64;
-constexpr int kPipeCW = 8;  // consumer warps
-constexpr int kPipeThreads = 32 * (kPipeCW + 1);
-constexpr uint32_t kPipeSpin = 1u << 22;
+constexpr int kPipeCW = 12;  // consumer warps; then one producer and one publisher warp
+constexpr int kPipeThreads = 32 * (kPipeCW + 2);
+constexpr int kPubSlots = 4;  // tiles the publisher may lag behind the consumers
+constexpr uint32_t kPipeSpin = 1u << 22;  // mbarrier polls
+constexpr uint32_t kFlagSpin = 1u << 22;  // neighbour-flag polls (~128 ns apart)
 
 struct PipeArgs {
-    int n, nb, R, G, nchunk, stages, stage_bytes, maxU, maxBlk, B, first;
-    const int4 *hdr;   // per group: {nu, tb0, nbk, rec_off}, {rec_len, run_off, nruns, nr}
-    const int4 *runs;  // {first block row, rows, first slot, 0}
+    int n, nb, R, G, nchunk, stages, stage_bytes, maxU, maxBlk, B, run_stride;
+    int k0, steps;     // steps k0 .. k0+steps-1 (k = 0 computes T_1 = X T_0)
+    const int4 *hdr;   // per group: {nu, tb0, nbk, rec_off}, {rec_len, -, nruns, nr}
+    const int4 *runs;  // run_stride per group: {first block row, rows, first slot, 0}
     const int32_t *rec;
-    const float *x32, *Tin;
-    float *Tout;
-    float2 *partial;
+    const int32_t *nbr_ptr, *nbr;  // neighbouring groups of each group (itself included)
+    const float *x32;
+    float *T0, *T1;    // step k reads T_k from (k even ? T0 : T1) and writes T_{k+1} to the other
+    float2 *partial;   // [steps][G][B][2] pairs; step k writes block k - k0
+    int32_t *flags;    // [G * nchunk] completed steps per tile (multi-step launch), or null
     int32_t *err;
 };
 
@@ -104,6 +125,25 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         : "memory");
 }
 
+__device__ __forceinline__ int ld_acquire(const int32_t *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int32_t *p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+// orders generic-proxy accesses to global memory with the bulk (async-proxy)
+// copies that follow
+__device__ __forceinline__ void fence_proxy_async_global()
+{
+    asm volatile("fence.proxy.async.global;\n" ::: "memory");
+}
+
 // (s, c) += x with the rounding error of s + x kept exactly in c (TwoSum)
 __device__ __forceinline__ void pair_add(float &s, float &c, float x)
 {
@@ -136,71 +176,156 @@ __device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity, volat
     return true;
 }
 
+// Producer warp: the flag word lane q watches for tile (chunk, g): neighbour
+// q of g (q < 32), or null.
+__device__ __forceinline__ const int32_t *neighbour_flag(const PipeArgs &a, int chunk, int g, int q)
+{
+    const int p0 = a.nbr_ptr[g], p1 = a.nbr_ptr[g + 1];
+    return p0 + q < p1 ? a.flags + (int64_t)chunk * a.G + a.nbr[p0 + q] : nullptr;
+}
+
+// Producer warp: wait until every neighbour tile of (chunk, g) has published
+// step k.  seen: this lane's flag as read (acquire) before the stage wait, so
+// that an already satisfied wait costs no further round trip.  Otherwise the
+// lanes poll the neighbours in parallel with acquire loads; false on abort /
+// timeout.
+__device__ __forceinline__ bool wait_neighbours(const PipeArgs &a, int chunk, int g, int k, int lane, int seen,
+                                                volatile int *s_abort)
+{
+    const int p0 = a.nbr_ptr[g], p1 = a.nbr_ptr[g + 1];
+    const int32_t *fl = a.flags + (int64_t)chunk * a.G;
+    if (p1 - p0 <= 32 && __all_sync(0xffffffffu, seen >= k)) return true;
+    for (int base = p0; base < p1; base += 32) {
+        const int q = base + lane;
+        const int32_t *f = q < p1 ? fl + a.nbr[q] : nullptr;
+        uint32_t n = 0;
+        while (!__all_sync(0xffffffffu, f == nullptr || ld_acquire(f) >= k)) {
+            if (*s_abort) return false;
+            if (++n >= kFlagSpin) {
+                if (lane == 0) {
+                    *s_abort = 1;
+                    atomicExch(a.err, 2);
+                }
+                __syncwarp();
+                return false;
+            }
+            __nanosleep(128);
+        }
+    }
+    return true;
+}
+
 __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    float *red = reinterpret_cast<float *>(smem + (size_t)a.stages * a.stage_bytes);  // [2][CW][64][2][2]
-    uint64_t *full = reinterpret_cast<uint64_t *>(red + 2 * kPipeCW * kPipeCols * 4);
+    float *red = reinterpret_cast<float *>(smem + (size_t)a.stages * a.stage_bytes);  // [CW][64][2][2]
+    uint64_t *full = reinterpret_cast<uint64_t *>(red + kPipeCW * kPipeCols * 4);
     uint64_t *empty = full + a.stages;
-    volatile int *s_abort = reinterpret_cast<volatile int *>(empty + a.stages);
+    uint64_t *pub = empty + a.stages;       // consumers -> publisher: tile done
+    uint64_t *pubfree = pub + kPubSlots;    // publisher -> consumers: slot free again
+    volatile int *s_abort = reinterpret_cast<volatile int *>(pubfree + kPubSlots);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         for (int s = 0; s < a.stages; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], kPipeCW);
         }
+        for (int s = 0; s < kPubSlots; s++) {
+            mbar_init(&pub[s], 1);
+            mbar_init(&pubfree[s], 1);
+        }
         *s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
     const int ntiles = a.G * a.nchunk;
+    const int mine = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int total = mine * a.steps;  // this CTA's tiles over all steps, step-major
     const int oT = 0, oP = a.maxU * 4 * kPipeCols, oX = oP + a.R * 4 * kPipeCols,
               oRec = oX + a.maxBlk * 16;  // float offsets inside a stage
     const int64_t chunk_floats = (int64_t)a.n * kPipeCols;
 
+    if (warp == kPipeCW + 1) {
+        // ---------------- publisher ----------------
+        // Publishes each finished tile's step count: a GPU-scope fence makes
+        // the consumers' T_{k+1} stores (ordered before the slot's mbarrier
+        // arrival) visible before the release store of the flag.  The fence
+        // stalls only this warp.
+        if (!a.flags) return;
+        for (int i = 0; i < total; ++i) {
+            const int s = i % kPubSlots;
+            if (!wait_phase(&pub[s], (uint32_t)(i / kPubSlots) & 1u, s_abort, a.err)) break;
+            if (lane == 0) {
+                const int k = a.k0 + i / mine;
+                const int t = (int)blockIdx.x + (i % mine) * (int)gridDim.x;
+                __threadfence();
+                fence_proxy_async_global();
+                st_release(a.flags + t, k + 1);
+                mbar_arrive(&pubfree[s]);
+            }
+            __syncwarp();
+        }
+        return;
+    }
+
     if (warp == kPipeCW) {
         // ---------------- producer ----------------
         int i = 0;
-        int t = blockIdx.x;
-        int4 ha = make_int4(0, 0, 0, 0), hb = ha;
-        if (t < ntiles) {
-            const int g = t % a.G;
+        int4 ha = make_int4(0, 0, 0, 0), hb = ha, run = ha;
+        if (total > 0) {
+            const int g = (int)blockIdx.x % a.G;
             ha = __ldg(a.hdr + 2 * g);
             hb = __ldg(a.hdr + 2 * g + 1);
+            run = __ldg(a.runs + (int64_t)g * a.run_stride + lane);
         }
-        for (; t < ntiles; t += gridDim.x, ++i) {
+        for (; i < total; ++i) {
+            const int k = a.k0 + i / mine;
+            const int t = (int)blockIdx.x + (i % mine) * (int)gridDim.x;
             const int chunk = t / a.G, g = t - chunk * a.G;
             const int nu = ha.x, tb0 = ha.y, nbk = ha.z, r0 = ha.w;
-            const int rl = hb.x, roff = hb.y, nruns = hb.z, nr = hb.w;
-            const int tn = t + gridDim.x;  // read the next tile's header now
-            if (tn < ntiles) {
+            const int rl = hb.x, nruns = hb.z, nr = hb.w;
+            const int4 cur = run;
+            if (i + 1 < total) {  // header and runs of the next tile
+                const int tn = (int)blockIdx.x + ((i + 1) % mine) * (int)gridDim.x;
                 const int gn = tn % a.G;
                 ha = __ldg(a.hdr + 2 * gn);
                 hb = __ldg(a.hdr + 2 * gn + 1);
+                run = __ldg(a.runs + (int64_t)gn * a.run_stride + lane);
             }
-            const int4 run = lane < nruns ? __ldg(a.runs + roff + lane) : make_int4(0, 0, 0, 0);
+            // this tile's neighbour flags, read before the stage wait
+            int seen = 0x7fffffff;
+            if (a.flags && k > 0) {
+                const int32_t *f = neighbour_flag(a, chunk, g, lane);
+                if (f) seen = ld_acquire(f);
+            }
             const int s = i % a.stages;
             if (i >= a.stages && !wait_phase(&empty[s], (uint32_t)((i / a.stages) - 1) & 1u, s_abort, a.err))
                 break;
+            if (a.flags && k > 0) {
+                if (!wait_neighbours(a, chunk, g, k, lane, seen, s_abort)) break;
+                fence_proxy_async_global();
+            }
+            const float *Tin = (k & 1) ? a.T1 : a.T0;
+            const float *Tprev = (k & 1) ? a.T0 : a.T1;
             float *stg = reinterpret_cast<float *>(smem + (size_t)s * a.stage_bytes);
             if (lane == 0)
-                mbar_arrive_expect_tx(&full[s], (uint32_t)nu * 1024u + (a.first ? 0u : (uint32_t)nr * 1024u) +
+                mbar_arrive_expect_tx(&full[s], (uint32_t)nu * 1024u + (k == 0 ? 0u : (uint32_t)nr * 1024u) +
                                                     (uint32_t)nbk * 64u + (uint32_t)rl * 4u);
             __syncwarp();
-            const float *srcT = a.Tin + (int64_t)chunk * chunk_floats;
+            const float *srcT = Tin + (int64_t)chunk * chunk_floats;
             if (lane < nruns)
-                bulk_g2s(stg + oT + run.z * 4 * kPipeCols, srcT + (int64_t)run.x * 4 * kPipeCols,
-                         (uint32_t)run.y * 1024u, &full[s]);
+                bulk_g2s(stg + oT + cur.z * 4 * kPipeCols, srcT + (int64_t)cur.x * 4 * kPipeCols,
+                         (uint32_t)cur.y * 1024u, &full[s]);
             for (int q = lane + 32; q < nruns; q += 32) {
-                const int4 rr = __ldg(a.runs + roff + q);
+                const int4 rr = __ldg(a.runs + (int64_t)g * a.run_stride + q);
                 bulk_g2s(stg + oT + rr.z * 4 * kPipeCols, srcT + (int64_t)rr.x * 4 * kPipeCols,
                          (uint32_t)rr.y * 1024u, &full[s]);
             }
             if (lane == 0) {
                 bulk_g2s(stg + oX, a.x32 + (int64_t)tb0 * 16, (uint32_t)nbk * 64u, &full[s]);
                 bulk_g2s(stg + oRec, a.rec + r0, (uint32_t)rl * 4u, &full[s]);
-                if (!a.first)
-                    bulk_g2s(stg + oP, a.Tout + (int64_t)chunk * chunk_floats + (int64_t)g * a.R * 4 * kPipeCols,
+                if (k > 0)
+                    bulk_g2s(stg + oP, Tprev + (int64_t)chunk * chunk_floats + (int64_t)g * a.R * 4 * kPipeCols,
                              (uint32_t)nr * 1024u, &full[s]);
             }
         }
@@ -217,11 +342,13 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
 
     // ---------------- consumers ----------------
     const int c = 2 * lane;
-    int i = 0, buf = 0;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i, buf ^= 1) {
+    for (int i = 0; i < total; ++i) {
+        const int k = a.k0 + i / mine;
+        const int t = (int)blockIdx.x + (i % mine) * (int)gridDim.x;
         const int s = i % a.stages;
         const int chunk = t / a.G, g = t - chunk * a.G;
         const int I0 = g * a.R, nr = min(a.nb, I0 + a.R) - I0;
+        float *out = ((k & 1) ? a.T0 : a.T1) + (int64_t)chunk * chunk_floats + (int64_t)I0 * 4 * kPipeCols + c;
         // pairs (hi, lo): [0] <T_k,T_k> col c, [1] <T_k,T_{k+1}> col c, [2], [3] the same for col c+1
         float hs[4] = {0.f, 0.f, 0.f, 0.f}, ls[4] = {0.f, 0.f, 0.f, 0.f};
         if (wait_phase(&full[s], (uint32_t)(i / a.stages) & 1u, s_abort, a.err)) {
@@ -230,7 +357,6 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
             const int32_t *sRp = reinterpret_cast<const int32_t *>(stg + oRec);
             const int32_t *sLc = sRp + nr + 1;
             const int32_t *sLs = sLc + sRp[nr];
-            float *out = a.Tout + (int64_t)chunk * chunk_floats + (int64_t)I0 * 4 * kPipeCols + c;
             for (int r = warp; r < nr; r += kPipeCW) {
                 float acc[4][2];
 #pragma unroll
@@ -259,7 +385,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                 for (int q = 0; q < 4; q++) {
                     const float2 ov = *reinterpret_cast<const float2 *>(own + q * kPipeCols);
                     float2 o;
-                    if (a.first) {
+                    if (k == 0) {
                         o = make_float2(acc[q][0], acc[q][1]);
                     } else {
                         const float2 p = *reinterpret_cast<const float2 *>(sP + (r * 4 + q) * kPipeCols + c);
@@ -280,21 +406,29 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);  // stage s may be refilled
-        float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)(buf * kPipeCW + warp) * kPipeCols + c) * 4);
+        if (i > 0) consumer_sync();             // the previous tile's sums have been read
+        float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)warp * kPipeCols + c) * 4);
         rb[0] = make_float4(hs[0], ls[0], hs[1], ls[1]);
         rb[1] = make_float4(hs[2], ls[2], hs[3], ls[3]);
-        consumer_sync();
-        if (tid < 2 * kPipeCols && !*s_abort) {
-            const int j = tid >> 1, which = tid & 1;
-            float hsum = 0.f, lsum = 0.f;
+        consumer_sync();  // also: every consumer's T_{k+1} stores of this tile precede it
+        if (!*s_abort) {
+            if (tid < 2 * kPipeCols) {
+                const int j = tid >> 1, which = tid & 1;
+                float hsum = 0.f, lsum = 0.f;
 #pragma unroll
-            for (int w = 0; w < kPipeCW; w++) {
-                const float2 v =
-                    *reinterpret_cast<const float2 *>(red + ((size_t)(buf * kPipeCW + w) * kPipeCols + j) * 4 + which * 2);
-                pair_add(hsum, lsum, v.x);
-                lsum += v.y;
+                for (int w = 0; w < kPipeCW; w++) {
+                    const float2 v = *reinterpret_cast<const float2 *>(red + ((size_t)w * kPipeCols + j) * 4 + which * 2);
+                    pair_add(hsum, lsum, v.x);
+                    lsum += v.y;
+                }
+                a.partial[(((int64_t)(k - a.k0) * a.G + g) * a.B + chunk * kPipeCols + j) * 2 + which] =
+                    make_float2(hsum, lsum);
             }
-            a.partial[((int64_t)g * a.B + chunk * kPipeCols + j) * 2 + which] = make_float2(hsum, lsum);
+        }
+        if (a.flags && tid == 0) {  // hand the tile to the publisher (also on abort: it returns)
+            const int ps = i % kPubSlots;
+            if (i < kPubSlots || wait_phase(&pubfree[ps], (uint32_t)((i / kPubSlots) - 1) & 1u, s_abort, a.err))
+                mbar_arrive(&pub[ps]);
         }
     }
 }
@@ -309,26 +443,6 @@ __global__ void k_slab_identity_cm(float *__restrict__ T0, int n, int B, int c0)
         const int row = (int)(rem / kPipeCols), j = (int)(rem % kPipeCols);
         T0[e] = (row == c0 + chunk * kPipeCols + j) ? 1.f : 0.f;
     }
-}
-
-}  // namespace
-
-size_t cheb_f32_pipe_stage_bytes(int R, int maxU, int maxBlk, int rec_cap)
-{
-    const size_t b = (size_t)(maxU + R) * 4 * kPipeCols * sizeof(float) + (size_t)maxBlk * 16 * sizeof(float) +
-                     (size_t)rec_cap * sizeof(int32_t);
-    return (b + 127) / 128 * 128;
-}
-
-size_t cheb_f32_pipe_smem(size_t stage_bytes, int stages)
-{
-    return (size_t)stages * stage_bytes + (size_t)2 * kPipeCW * kPipeCols * 4 * sizeof(float) +
-           (size_t)2 * stages * sizeof(uint64_t) + 16;
-}
-
-int cheb_f32_pipe_configure(size_t smem)
-{
-    return (int)cudaFuncSetAttribute(k_cheb_f32_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 // Sum the per-group (hi, lo) pairs of a slab in FP32 pairs, convert once to
@@ -356,11 +470,29 @@ __global__ void k_f32_finalize_pairs(const float2 *__restrict__ partial, int K, 
     if (2 * k + 1 <= M) d[(int64_t)(2 * k + 1) * n + i] = 2.0 * so - (double)xdiag32[i];
 }
 
-void launch_slab_identity_cm(cudaStream_t st, float *T0, int n, int B, int c0)
+}  // namespace
+
+size_t cheb_f32_pipe_stage_bytes(int R, int maxU, int maxBlk, int rec_cap)
 {
-    const int64_t tot = (int64_t)n * B;
-    const int blocks = (int)std::min<int64_t>((tot + 255) / 256, 152 * 16);
-    k_slab_identity_cm<<<blocks, 256, 0, st>>>(T0, n, B, c0);
+    const size_t b = (size_t)(maxU + R) * 4 * kPipeCols * sizeof(float) + (size_t)maxBlk * 16 * sizeof(float) +
+                     (size_t)rec_cap * sizeof(int32_t);
+    return (b + 127) / 128 * 128;
+}
+
+size_t cheb_f32_pipe_smem(size_t stage_bytes, int stages)
+{
+    return (size_t)stages * stage_bytes + (size_t)kPipeCW * kPipeCols * 4 * sizeof(float) +
+           (size_t)(2 * stages + 2 * kPubSlots) * sizeof(uint64_t) + 16;
+}
+
+int cheb_f32_pipe_max_rows() { return kPipeCW * 3; }
+
+int cheb_f32_pipe_configure(size_t smem, int *ctas_per_sm)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_cheb_f32_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    *ctas_per_sm = 0;
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_cheb_f32_pipe, kPipeThreads, smem);
 }
 
 void launch_f32_finalize_pairs(cudaStream_t st, const DevMatrix &m, const float2 *partial, int K, int rowgroups,
@@ -370,33 +502,53 @@ void launch_f32_finalize_pairs(cudaStream_t st, const DevMatrix &m, const float2
     k_f32_finalize_pairs<<<grid, 128, 0, st>>>(partial, K, rowgroups, B, c0, m.n, m.xdiag32, d, M);
 }
 
-int launch_cheb_step_f32_pipe(cudaStream_t st, const DevMatrix &m, const PipePlan &sp, const float *Tin,
-                              float *Tout, int B, int first, float2 *partial_k)
+void launch_slab_identity_cm(cudaStream_t st, float *T0, int n, int B, int c0)
+{
+    const int64_t tot = (int64_t)n * B;
+    const int blocks = (int)std::min<int64_t>((tot + 255) / 256, 152 * 16);
+    k_slab_identity_cm<<<blocks, 256, 0, st>>>(T0, n, B, c0);
+}
+
+int launch_cheb_f32_pipe(cudaStream_t st, const DevMatrix &m, const PipePlan &pl, float *T0, float *T1, int B,
+                         int k0, int steps, float2 *partial, bool multi)
 {
     PipeArgs a;
     a.n = m.n;
     a.nb = m.nb;
-    a.R = sp.R;
-    a.G = sp.G;
+    a.R = pl.R;
+    a.G = pl.G;
     a.nchunk = B / kPipeCols;
-    a.stages = sp.stages;
-    a.stage_bytes = (int)sp.stage_bytes;
-    a.maxU = sp.maxU;
-    a.maxBlk = sp.maxBlk;
+    a.stages = pl.stages;
+    a.stage_bytes = (int)pl.stage_bytes;
+    a.maxU = pl.maxU;
+    a.maxBlk = pl.maxBlk;
     a.B = B;
-    a.first = first;
-    a.hdr = reinterpret_cast<const int4 *>(sp.hdr);
-    a.runs = reinterpret_cast<const int4 *>(sp.runs);
-    a.rec = sp.rec;
+    a.run_stride = pl.run_stride;
+    a.k0 = k0;
+    a.steps = steps;
+    a.hdr = reinterpret_cast<const int4 *>(pl.hdr);
+    a.runs = reinterpret_cast<const int4 *>(pl.runs);
+    a.rec = pl.rec;
+    a.nbr_ptr = pl.nbr_ptr;
+    a.nbr = pl.nbr;
     a.x32 = m.x32;
-    a.Tin = Tin;
-    a.Tout = Tout;
-    a.partial = partial_k;
-    a.err = sp.err;
-    const int ntiles = sp.G * a.nchunk;
-    const int grid = std::min(ntiles, sp.nsm);
-    k_cheb_f32_pipe<<<grid, kPipeThreads, cheb_f32_pipe_smem(sp.stage_bytes, sp.stages), st>>>(a);
-    return 1;
+    a.T0 = T0;
+    a.T1 = T1;
+    a.partial = partial;
+    a.flags = multi ? pl.flags : nullptr;
+    a.err = pl.err;
+    const int ntiles = pl.G * a.nchunk;
+    const int grid = std::min(ntiles, pl.nsm);
+    const size_t smem = cheb_f32_pipe_smem(pl.stage_bytes, pl.stages);
+    if (!multi) {
+        k_cheb_f32_pipe<<<grid, kPipeThreads, smem, st>>>(a);
+        return (int)cudaSuccess;
+    }
+    cudaError_t e = cudaMemsetAsync(pl.flags, 0, sizeof(int32_t) * (size_t)ntiles, st);
+    if (e != cudaSuccess) return (int)e;
+    void *args[] = {&a};
+    return (int)cudaLaunchCooperativeKernel((const void *)k_cheb_f32_pipe, dim3(grid), dim3(kPipeThreads), args,
+                                            smem, st);
 }
 
 }  // namespace tb

@@ -239,11 +239,12 @@ def test_full_size_fp32_vs_fp64_properties(gpu):
     assert np.all(out[0]["diagP"] > -1e-6) and np.all(out[0]["diagP"] < 1 + 1e-6)
 
 
-@pytest.mark.parametrize("kern", [1, 2, 3])
+@pytest.mark.parametrize("kern", [1, 2, 3, 4])
 @pytest.mark.parametrize("dims,B", [((2, 2, 2), 0), ((1, 2, 3), 0), ((2, 2, 2), 128), ((1, 1, 3), 256)])
 def test_fp32_step_kernels_match_oracle(gpu, kern, dims, B):
-    """Each FP32 step kernel (staged, persistent, pipelined), forced, with the
-    autotuned and with fixed slab widths, against the FP64 oracle."""
+    """Each FP32 step kernel (staged, persistent, pipelined with one launch per
+    slab, pipelined with one launch per step), forced, with the autotuned and
+    with fixed slab widths, against the FP64 oracle."""
     m, o = _pair(*dims, seed=23)
     ref = O.density(o, O.kpe_params(M=160, kT=0.01, n_elec=o.n_elec))
     with _ctx(gpu, m, M=160, precision=gpu.PREC_FP32, fp32_kernel=kern, column_block=B) as c:
@@ -264,11 +265,14 @@ def test_pipelined_equals_staged_recurrence(gpu):
     import largetb_gb300 as T
     m = T.model_cristobalite(3, 3, 3, sigma_ang=0.08, seed=31)
     out = {}
-    for kern in (1, 3):
+    for kern in (1, 3, 4):
         with _ctx(gpu, m, M=300, precision=gpu.PREC_FP32, fp32_kernel=kern, column_block=512) as c:
             out[kern] = c.density()
-    assert np.abs(out[1]["q"] - out[3]["q"]).max() < 1e-10
-    np.testing.assert_allclose(out[1]["moments"], out[3]["moments"], rtol=0, atol=1e-9 * m.n)
+    for kern in (3, 4):
+        assert np.abs(out[1]["q"] - out[kern]["q"]).max() < 1e-10
+        np.testing.assert_allclose(out[1]["moments"], out[kern]["moments"], rtol=0, atol=1e-9 * m.n)
+    # the two pipelined modes run identical arithmetic in the same order
+    assert np.array_equal(out[3]["moments"], out[4]["moments"])
 
 
 def test_autotuner_reports_a_kernel(gpu):
@@ -277,5 +281,5 @@ def test_autotuner_reports_a_kernel(gpu):
     with _ctx(gpu, m, M=60, precision=gpu.PREC_FP32) as c:
         rep = c.density()["report"]
         again = c.density()["report"]
-    assert rep["step_kernel"] in (1, 2, 3)
+    assert rep["step_kernel"] in (1, 2, 3, 4)
     assert (again["step_kernel"], again["column_block"]) == (rep["step_kernel"], rep["column_block"])
