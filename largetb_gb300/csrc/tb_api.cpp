@@ -249,8 +249,8 @@ int autotune(tb_ctx *ctx, int req)
             cudaEventRecord(a, st);
             if (cd.kind == kKindPersistent) {
                 cudaMemsetAsync(ctx->pp.flags, 0, sizeof(int32_t) * ctx->pp.G * ctx->pp.nc, st);
-                launch_cheb_f32_persistent(st, m, ctx->pp, kTuneSteps, B, 0, (float *)T0, (float *)T1, part,
-                                           ctx->pp.flags, ctx->pp.err);
+                launch_cheb_f32_persistent(st, m, ctx->pp, kTuneSteps, B, 0, (float *)T0, (float *)T1,
+                                           reinterpret_cast<float2 *>(part), ctx->pp.flags, ctx->pp.err);
             } else if (cd.kind == kKindPipelined) {
                 launch_slab_identity_cm(st, (float *)T0, m.n, B, 0);
                 const int e = launch_cheb_f32_pipe(st, m, ctx->pl, (float *)T0, (float *)T1, B, 0, kTuneSteps,
@@ -273,9 +273,11 @@ int autotune(tb_ctx *ctx, int req)
                         launch_cheb_f32_pipe(st, m, ctx->pl, (float *)T0, (float *)T1, B, k, 1,
                                              reinterpret_cast<float2 *>(pk), false);
                     else if (ctx->sp.R > 0)
-                        launch_cheb_step_f32_staged(st, m, ctx->sp, (float *)in, (float *)out, B, k == 0, pk);
+                        launch_cheb_step_f32_staged(st, m, ctx->sp, (float *)in, (float *)out, B, k == 0,
+                                                    reinterpret_cast<float2 *>(pk));
                     else
-                        launch_cheb_step_f32(st, m, (float *)in, (float *)out, B, k == 0, pk, rowgroups);
+                        launch_cheb_step_f32(st, m, (float *)in, (float *)out, B, k == 0,
+                                             reinterpret_cast<float2 *>(pk), rowgroups);
                 }
             }
             cudaEventRecord(b, st);
@@ -780,12 +782,13 @@ int density_eval(tb_ctx *ctx, bool have_shift)
         } else if (w.kind == kKindPersistent) {
             TB_CUDA(cudaMemsetAsync(ctx->pp.flags, 0, sizeof(int32_t) * ctx->pp.G * ctx->pp.nc, st));
             const int e = launch_cheb_f32_persistent(st, m, ctx->pp, w.K, B, c0, (float *)w.T0,
-                                                     (float *)w.T1, w.partial, ctx->pp.flags,
-                                                     ctx->pp.err);
+                                                     (float *)w.T1, reinterpret_cast<float2 *>(w.partial),
+                                                     ctx->pp.flags, ctx->pp.err);
             if (e != (int)cudaSuccess)
                 return fail(ctx, TB_ERR_CUDA,
                             std::string("cooperative launch: ") + cudaGetErrorString((cudaError_t)e));
-            launch_f32_finalize(st, m, w.partial, w.K, w.rowgroups, B, c0, w.d, M);
+            launch_f32_finalize_pairs(st, m, reinterpret_cast<const float2 *>(w.partial), w.K, w.rowgroups, B, c0,
+                                      w.d, M);
             ctx->launches += 2;
             ctx->spmm_launches += w.K;  // one launch carries all K slab steps
             ctx->spmm_bytes += w.K * step_bytes(m, B, 4);
@@ -798,16 +801,15 @@ int density_eval(tb_ctx *ctx, bool have_shift)
                 if (w.kind == kKindPipelinedStep)
                     launch_cheb_f32_pipe(st, m, ctx->pl, A, Bf, B, k, 1, reinterpret_cast<float2 *>(pk), false);
                 else if (ctx->sp.R > 0)
-                    launch_cheb_step_f32_staged(st, m, ctx->sp, odd ? A : Bf, odd ? Bf : A, B, k == 0, pk);
+                    launch_cheb_step_f32_staged(st, m, ctx->sp, odd ? A : Bf, odd ? Bf : A, B, k == 0,
+                                                reinterpret_cast<float2 *>(pk));
                 else
-                    launch_cheb_step_f32(st, m, odd ? A : Bf, odd ? Bf : A, B, k == 0, pk, w.rowgroups);
+                    launch_cheb_step_f32(st, m, odd ? A : Bf, odd ? Bf : A, B, k == 0,
+                                         reinterpret_cast<float2 *>(pk), w.rowgroups);
                 ctx->launches++;
             }
-            if (w.kind == kKindPipelinedStep)
-                launch_f32_finalize_pairs(st, m, reinterpret_cast<const float2 *>(w.partial), w.K, w.rowgroups, B,
-                                          c0, w.d, M);
-            else
-                launch_f32_finalize(st, m, w.partial, w.K, w.rowgroups, B, c0, w.d, M);
+            launch_f32_finalize_pairs(st, m, reinterpret_cast<const float2 *>(w.partial), w.K, w.rowgroups, B, c0,
+                                      w.d, M);
             ctx->launches++;
             ctx->spmm_launches += w.K;
             ctx->spmm_bytes += w.K * step_bytes(m, B, 4);

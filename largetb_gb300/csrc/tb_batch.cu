@@ -177,6 +177,18 @@ __global__ void k_bt_identity(const Unit *__restrict__ units, int nunits, const 
     }
 }
 
+// (s, c) += x with the rounding error of s + x kept exactly in c (Knuth's
+// TwoSum): column dot products accumulate as FP32 pairs, since GB300 issues
+// FP64 at only about 2 operations per clock per SM.
+__device__ __forceinline__ void pair_add(float &s, float &c, float x)
+{
+    const float t = s + x;
+    const float bp = t - s;
+    const float e = (s - (t - bp)) + (x - bp);
+    s = t;
+    c += e;
+}
+
 // ---- one FP32 Chebyshev step for every unit (staged as k_cheb_f32_staged) ----
 __global__ void __launch_bounds__(32 * kBtWarps)
     k_bt_cheb_f32(const Unit *__restrict__ units, const int32_t *__restrict__ s_ao,
@@ -186,7 +198,7 @@ __global__ void __launch_bounds__(32 * kBtWarps)
                   const int32_t *__restrict__ lcol, const int32_t *__restrict__ lself,
                   const int32_t *__restrict__ grp_ptr, const int32_t *__restrict__ grp_rows,
                   const float *__restrict__ x32, const float *__restrict__ Tin_base,
-                  float *__restrict__ Tout_base, int first, double *__restrict__ partial, int maxU,
+                  float *__restrict__ Tout_base, int first, float2 *__restrict__ partial, int maxU,
                   int maxBlk)
 {
     extern __shared__ float4 bsm4[];
@@ -223,7 +235,8 @@ __global__ void __launch_bounds__(32 * kBtWarps)
     cpa_wait();
     __syncthreads();
     const int lane = tid & 31, w = tid >> 5, c = 2 * lane;
-    double see[2] = {0.0, 0.0}, seo[2] = {0.0, 0.0};
+    // pairs (hi, lo): <T_k,T_k> and <T_k,T_{k+1}> of columns c and c+1
+    float hs[4] = {0.f, 0.f, 0.f, 0.f}, ls[4] = {0.f, 0.f, 0.f, 0.f};
     for (int r = w; r < nr; r += kBtWarps) {
         const int I = I0 + r;
         float acc[4][2];
@@ -265,24 +278,27 @@ __global__ void __launch_bounds__(32 * kBtWarps)
             eo[0] = fmaf(ov.x, o.x, eo[0]);
             eo[1] = fmaf(ov.y, o.y, eo[1]);
         }
-        see[0] += (double)ee[0];
-        see[1] += (double)ee[1];
-        seo[0] += (double)eo[0];
-        seo[1] += (double)eo[1];
+        pair_add(hs[0], ls[0], ee[0]);
+        pair_add(hs[1], ls[1], eo[0]);
+        pair_add(hs[2], ls[2], ee[1]);
+        pair_add(hs[3], ls[3], eo[1]);
     }
     __syncthreads();
-    double *red = reinterpret_cast<double *>(bsm4);
-    red[(w * kBtCols + c) * 2 + 0] = see[0];
-    red[(w * kBtCols + c) * 2 + 1] = seo[0];
-    red[(w * kBtCols + c + 1) * 2 + 0] = see[1];
-    red[(w * kBtCols + c + 1) * 2 + 1] = seo[1];
+    float *red = reinterpret_cast<float *>(bsm4);  // [warp][col][which][hi, lo]
+    float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)w * kBtCols + c) * 4);
+    rb[0] = make_float4(hs[0], ls[0], hs[1], ls[1]);
+    rb[1] = make_float4(hs[2], ls[2], hs[3], ls[3]);
     __syncthreads();
     if (tid < 2 * kBtCols) {
         const int j = tid >> 1, which = tid & 1;
-        double sacc = 0.0;
+        float hsum = 0.f, lsum = 0.f;
 #pragma unroll
-        for (int q = 0; q < kBtWarps; q++) sacc += red[(q * kBtCols + j) * 2 + which];
-        partial[s_poff[s] + ((int64_t)(g - s_g0[s]) * B + col0 + j) * 2 + which] = sacc;
+        for (int q = 0; q < kBtWarps; q++) {
+            const float2 v = *reinterpret_cast<const float2 *>(red + ((size_t)q * kBtCols + j) * 4 + which * 2);
+            pair_add(hsum, lsum, v.x);
+            lsum += v.y;
+        }
+        partial[s_poff[s] + ((int64_t)(g - s_g0[s]) * B + col0 + j) * 2 + which] = make_float2(hsum, lsum);
     }
 }
 
@@ -290,7 +306,7 @@ __global__ void __launch_bounds__(32 * kBtWarps)
 __global__ void k_bt_finalize(int n_total, int k, int M, const int32_t *__restrict__ s_of_atom,
                               const int32_t *__restrict__ active, const int32_t *__restrict__ s_ao,
                               const int32_t *__restrict__ s_B, const int64_t *__restrict__ s_poff,
-                              const int32_t *__restrict__ s_g0, const double *__restrict__ partial,
+                              const int32_t *__restrict__ s_g0, const float2 *__restrict__ partial,
                               const float *__restrict__ xdiag32, double *__restrict__ d)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -298,12 +314,16 @@ __global__ void k_bt_finalize(int n_total, int k, int M, const int32_t *__restri
     const int s = s_of_atom[i >> 2];
     if (!active[s]) return;
     const int j = i - 4 * s_ao[s], B = s_B[s], G = s_g0[s + 1] - s_g0[s];
-    const double *p = partial + s_poff[s];
-    double se = 0.0, so = 0.0;
+    const float2 *p = partial + s_poff[s];
+    float eh = 0.f, el = 0.f, oh = 0.f, ol = 0.f;
     for (int g = 0; g < G; g++) {
-        se += p[((int64_t)g * B + j) * 2 + 0];
-        so += p[((int64_t)g * B + j) * 2 + 1];
+        const float2 e = p[((int64_t)g * B + j) * 2 + 0], o = p[((int64_t)g * B + j) * 2 + 1];
+        pair_add(eh, el, e.x);
+        el += e.y;
+        pair_add(oh, ol, o.x);
+        ol += o.y;
     }
+    const double se = (double)eh + (double)el, so = (double)oh + (double)ol;
     if (2 * k <= M) d[(int64_t)(2 * k) * n_total + i] = 2.0 * se - 1.0;
     if (2 * k + 1 <= M) d[(int64_t)(2 * k + 1) * n_total + i] = 2.0 * so - (double)xdiag32[i];
 }
@@ -639,7 +659,7 @@ size_t bt_smem(int maxU, int maxBlk)
 {
     const size_t b = (size_t)(maxU * 4 * kBtCols + kBtR * 4 * kBtCols + maxBlk * 16) * sizeof(float) +
                      (size_t)(maxU + maxBlk + kBtR + 1) * sizeof(int);
-    const size_t red = (size_t)kBtWarps * kBtCols * 2 * sizeof(double);
+    const size_t red = (size_t)kBtWarps * kBtCols * 4 * sizeof(float);  // FP32 pairs of 2 sums per column
     return std::max(b, red);
 }
 
@@ -1020,9 +1040,12 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
             k_bt_cheb_f32<<<nu, 32 * kBtWarps, smem, st>>>(b->units, b->s_ao, b->s_B, b->s_toff, b->s_poff,
                                                             b->s_g0, b->grp_I0, b->rowptr, b->lcol, b->lself,
                                                             b->grp_ptr, b->grp_rows, b->x32, Tin, Tout, k == 0,
-                                                            b->partial, b->maxU, b->maxBlk);
+                                                            reinterpret_cast<float2 *>(b->partial), b->maxU,
+                                                            b->maxBlk);
             k_bt_finalize<<<(n + 255) / 256, 256, 0, st>>>(n, k, M, b->s_of_atom, b->active, b->s_ao, b->s_B,
-                                                           b->s_poff, b->s_g0, b->partial, b->xdiag32, b->d);
+                                                           b->s_poff, b->s_g0,
+                                                           reinterpret_cast<const float2 *>(b->partial),
+                                                           b->xdiag32, b->d);
             launches += 2;
         }
         cudaEventRecord(m1, st);

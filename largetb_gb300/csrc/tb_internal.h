@@ -128,7 +128,7 @@ struct DevWork {
     double *cand = nullptr;    // kBisectCand electron counts
     double *diagP = nullptr;   // n
     double *q = nullptr;       // natoms
-    double *partial = nullptr; // FP32 form: K * rowgroups * B * 2 dot partials
+    double *partial = nullptr; // FP32 form: K * rowgroups * B * 2 dot-product slots, each a float2 (hi, lo)
     void *T0 = nullptr, *T1 = nullptr;  // slab buffers, n x B
     size_t slab_bytes = 0;
     int64_t partial_elems = 0;
@@ -182,14 +182,14 @@ void launch_cheb_step_f64(cudaStream_t st, const DevMatrix &m, const double *Tin
                           int B, int c0, int first, double *d, int kout);
 // One FP32 step with the fused column dot products of T_k.
 void launch_cheb_step_f32(cudaStream_t st, const DevMatrix &m, const float *Tin, float *Tout,
-                          int B, int first, double *partial_k, int rowgroups);
+                          int B, int first, float2 *partial_k, int rowgroups);
 int cheb_f32_rowgroups(int nb);
 size_t cheb_f32_staged_smem(int R, int maxU, int maxBlk);
 int cheb_f32_staged_configure(size_t smem);  // returns a cudaError_t
 size_t cheb_f32_persistent_smem(int R, int maxH, int maxBlk, int maxNG);
 int cheb_f32_persistent_setup(int R, size_t smem, int *ctas_per_sm);  // returns a cudaError_t
 int launch_cheb_f32_persistent(cudaStream_t st, const DevMatrix &m, const PersistPlan &pp, int K,
-                               int B, int c0, float *G0, float *G1, double *partial, int *flags,
+                               int B, int c0, float *G0, float *G1, float2 *partial, int *flags,
                                int *err);  // returns a cudaError_t
 // ---- tb_pipe.cu ----
 size_t cheb_f32_pipe_stage_bytes(int R, int maxU, int maxBlk, int rec_cap);
@@ -208,9 +208,7 @@ void launch_f32_finalize_pairs(cudaStream_t st, const DevMatrix &m, const float2
                                int B, int c0, double *d, int M);
 int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const StagePlan &sp,
                                 const float *Tin, float *Tout, int B, int first,
-                                double *partial_k);
-void launch_f32_finalize(cudaStream_t st, const DevMatrix &m, const double *partial, int K,
-                         int rowgroups, int B, int c0, double *d, int M);
+                                float2 *partial_k);
 void launch_moment_sums(cudaStream_t st, const double *d, int n, int nmom, double *mom);
 void launch_dos_nodes(cudaStream_t st, const double *g, const double *mom, int M,
                       const DevState *state, int nq_cap, double *rho);

@@ -306,13 +306,26 @@ void launch_cheb_step_f64(cudaStream_t st, const DevMatrix &m, const double *Tin
                                                 B, c0, first, d, kout);
 }
 
+// (s, c) += x with the rounding error of s + x kept exactly in c (Knuth's
+// TwoSum).  The FP32 step kernels accumulate their column dot products as
+// such FP32 pairs across block rows and warps and write (hi, lo) pairs; GB300
+// issues FP64 at only about 2 operations per clock per SM.
+__device__ __forceinline__ void pair_add(float &s, float &c, float x)
+{
+    const float t = s + x;
+    const float bp = t - s;
+    const float e = (s - (t - bp)) + (x - bp);
+    s = t;
+    c += e;
+}
+
 // ---------------------------------------------------------------------------
 // FP32 Chebyshev step with fused column dot products.
 // CTA = 8 warps sharing one 128-column chunk; warp w handles kRowsPerWarp
 // consecutive block rows; lane = 4 columns (float4).  For every column j the
 // CTA accumulates  <T_k, T_k>  and  <T_k, T_{k+1}>  over its rows (FP32 per
-// block row, FP64 across block rows and warps) and writes one FP64 partial
-// pair per column to partial_k[rowgroup][B][2].
+// block row, FP32 pairs across block rows and warps) and writes one (hi, lo)
+// pair per sum and column to partial_k[rowgroup][B][2].
 // ---------------------------------------------------------------------------
 constexpr int kF32Warps = 8;
 constexpr int kRowsPerWarp = 2;
@@ -320,14 +333,14 @@ constexpr int kRowsPerWarp = 2;
 __global__ void __launch_bounds__(32 * kF32Warps)
     k_cheb_f32(int nb, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ colidx,
                const float *__restrict__ x32, const float *__restrict__ Tin,
-               float *__restrict__ Tout, int B, int first, double *__restrict__ partial_k)
+               float *__restrict__ Tout, int B, int first, float2 *__restrict__ partial_k)
 {
-    __shared__ double red[kF32Warps][128][2];
+    __shared__ __align__(16) float red[kF32Warps][128][4];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int chunk = blockIdx.y;
     const int col = chunk * 128 + lane * 4;
     const int Ibase = (blockIdx.x * kF32Warps + w) * kRowsPerWarp;
-    double see[4] = {0, 0, 0, 0}, seo[4] = {0, 0, 0, 0};
+    float hee[4] = {0, 0, 0, 0}, lee[4] = {0, 0, 0, 0}, heo[4] = {0, 0, 0, 0}, leo[4] = {0, 0, 0, 0};
 #pragma unroll 1
     for (int rr = 0; rr < kRowsPerWarp; rr++) {
         const int I = Ibase + rr;
@@ -395,22 +408,23 @@ __global__ void __launch_bounds__(32 * kF32Warps)
         }
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-            see[c] += (double)ee[c];
-            seo[c] += (double)eo[c];
+            pair_add(hee[c], lee[c], ee[c]);
+            pair_add(heo[c], leo[c], eo[c]);
         }
     }
 #pragma unroll
-    for (int c = 0; c < 4; c++) {
-        red[w][lane * 4 + c][0] = see[c];
-        red[w][lane * 4 + c][1] = seo[c];
-    }
+    for (int c = 0; c < 4; c++)
+        *reinterpret_cast<float4 *>(red[w][lane * 4 + c]) = make_float4(hee[c], lee[c], heo[c], leo[c]);
     __syncthreads();
     {
         const int j = threadIdx.x >> 1, which = threadIdx.x & 1;  // 256 threads = 128 cols x 2
-        double s = 0.0;
+        float hs = 0.f, ls = 0.f;
 #pragma unroll
-        for (int q = 0; q < kF32Warps; q++) s += red[q][j][which];
-        partial_k[((int64_t)blockIdx.x * B + chunk * 128 + j) * 2 + which] = s;
+        for (int q = 0; q < kF32Warps; q++) {
+            pair_add(hs, ls, red[q][j][2 * which]);
+            ls += red[q][j][2 * which + 1];
+        }
+        partial_k[((int64_t)blockIdx.x * B + chunk * 128 + j) * 2 + which] = make_float2(hs, ls);
     }
 }
 
@@ -421,7 +435,7 @@ int cheb_f32_rowgroups(int nb)
 }
 
 void launch_cheb_step_f32(cudaStream_t st, const DevMatrix &m, const float *Tin, float *Tout,
-                          int B, int first, double *partial_k, int rowgroups)
+                          int B, int first, float2 *partial_k, int rowgroups)
 {
     dim3 grid(rowgroups, B / 128);
     k_cheb_f32<<<grid, 32 * kF32Warps, 0, st>>>(m.nb, m.rowptr, m.colidx, m.x32, Tin, Tout, B,
@@ -457,7 +471,7 @@ __global__ void __launch_bounds__(32 * kV2Warps)
                       const int32_t *__restrict__ lcol, const int32_t *__restrict__ lself,
                       const int32_t *__restrict__ grp_ptr, const int32_t *__restrict__ grp_rows,
                       const float *__restrict__ x32, const float *__restrict__ Tin,
-                      float *__restrict__ Tout, int B, int first, double *__restrict__ partial_k,
+                      float *__restrict__ Tout, int B, int first, float2 *__restrict__ partial_k,
                       int maxU, int maxBlk)
 {
     extern __shared__ float4 smem4[];
@@ -497,7 +511,7 @@ __global__ void __launch_bounds__(32 * kV2Warps)
     __syncthreads();
     // ---- compute ----
     const int lane = tid & 31, w = tid >> 5, c = 2 * lane;
-    double see[2] = {0.0, 0.0}, seo[2] = {0.0, 0.0};
+    float hs[4] = {0.f, 0.f, 0.f, 0.f}, ls[4] = {0.f, 0.f, 0.f, 0.f};  // ee c, eo c, ee c+1, eo c+1
     for (int r = w; r < nr; r += kV2Warps) {
         const int I = I0 + r;
         const int ta = sR[r], te = sR[r + 1];
@@ -540,24 +554,27 @@ __global__ void __launch_bounds__(32 * kV2Warps)
             eo[0] = fmaf(ov.x, o.x, eo[0]);
             eo[1] = fmaf(ov.y, o.y, eo[1]);
         }
-        see[0] += (double)ee[0];
-        see[1] += (double)ee[1];
-        seo[0] += (double)eo[0];
-        seo[1] += (double)eo[1];
+        pair_add(hs[0], ls[0], ee[0]);
+        pair_add(hs[1], ls[1], eo[0]);
+        pair_add(hs[2], ls[2], ee[1]);
+        pair_add(hs[3], ls[3], eo[1]);
     }
     __syncthreads();  // shared T no longer needed: reuse for the reduction
-    double *red = reinterpret_cast<double *>(smem4);  // [8][64][2]
-    red[(w * kV2Cols + c) * 2 + 0] = see[0];
-    red[(w * kV2Cols + c) * 2 + 1] = seo[0];
-    red[(w * kV2Cols + c + 1) * 2 + 0] = see[1];
-    red[(w * kV2Cols + c + 1) * 2 + 1] = seo[1];
+    float *red = reinterpret_cast<float *>(smem4);  // [8][64][2 sums][hi, lo]
+    float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)w * kV2Cols + c) * 4);
+    rb[0] = make_float4(hs[0], ls[0], hs[1], ls[1]);
+    rb[1] = make_float4(hs[2], ls[2], hs[3], ls[3]);
     __syncthreads();
     if (tid < 2 * kV2Cols) {
         const int j = tid >> 1, which = tid & 1;
-        double sacc = 0.0;
+        float hsum = 0.f, lsum = 0.f;
 #pragma unroll
-        for (int q = 0; q < kV2Warps; q++) sacc += red[(q * kV2Cols + j) * 2 + which];
-        partial_k[((int64_t)g * B + col0 + j) * 2 + which] = sacc;
+        for (int q = 0; q < kV2Warps; q++) {
+            const float2 v = *reinterpret_cast<const float2 *>(red + ((size_t)q * kV2Cols + j) * 4 + which * 2);
+            pair_add(hsum, lsum, v.x);
+            lsum += v.y;
+        }
+        partial_k[((int64_t)g * B + col0 + j) * 2 + which] = make_float2(hsum, lsum);
     }
 }
 
@@ -571,13 +588,13 @@ size_t cheb_f32_staged_smem(int R, int maxU, int maxBlk)
 {
     size_t b = (size_t)(maxU * 4 * kV2Cols + R * 4 * kV2Cols + maxBlk * 16) * sizeof(float) +
                (size_t)(maxU + maxBlk + R + 1) * sizeof(int);
-    const size_t red = (size_t)kV2Warps * kV2Cols * 2 * sizeof(double);
+    const size_t red = (size_t)kV2Warps * kV2Cols * 4 * sizeof(float);
     return b > red ? b : red;
 }
 
 int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const StagePlan &sp,
                                 const float *Tin, float *Tout, int B, int first,
-                                double *partial_k)
+                                float2 *partial_k)
 {
     const size_t smem = cheb_f32_staged_smem(sp.R, sp.maxU, sp.maxBlk);
     dim3 grid(sp.G, B / kV2Cols);
@@ -624,7 +641,7 @@ __global__ void __launch_bounds__(32 * kPWarps, (kRPW <= 4 ? 3 : 2))
                           const int32_t *__restrict__ lcode, const int32_t *__restrict__ hptr,
                           const int32_t *__restrict__ hrows, const int32_t *__restrict__ nptr,
                           const int32_t *__restrict__ ngrp, const float *__restrict__ x32,
-                          float *__restrict__ G0, float *__restrict__ G1, double *__restrict__ partial,
+                          float *__restrict__ G0, float *__restrict__ G1, float2 *__restrict__ partial,
                           int G, int *__restrict__ flags, int *__restrict__ err, int maxH, int maxBlk,
                           int maxNG)
 {
@@ -744,7 +761,7 @@ __global__ void __launch_bounds__(32 * kPWarps, (kRPW <= 4 ? 3 : 2))
         cp_async_wait_all();
         __syncthreads();
         // ---- 4. halo contributions, T_{k+1} for the own rows, dot products ----
-        double see[2] = {0.0, 0.0}, seo[2] = {0.0, 0.0};
+        float hs[4] = {0.f, 0.f, 0.f, 0.f}, ls[4] = {0.f, 0.f, 0.f, 0.f};  // ee c, eo c, ee c+1, eo c+1
 #pragma unroll
         for (int j = 0; j < kRPW; j++) {
             const int r = w + j * kPWarps;
@@ -788,28 +805,31 @@ __global__ void __launch_bounds__(32 * kPWarps, (kRPW <= 4 ? 3 : 2))
                 eo[0] = fmaf(ov.x, o.x, eo[0]);
                 eo[1] = fmaf(ov.y, o.y, eo[1]);
             }
-            see[0] += (double)ee[0];
-            see[1] += (double)ee[1];
-            seo[0] += (double)eo[0];
-            seo[1] += (double)eo[1];
+            pair_add(hs[0], ls[0], ee[0]);
+            pair_add(hs[1], ls[1], eo[0]);
+            pair_add(hs[2], ls[2], ee[1]);
+            pair_add(hs[3], ls[3], eo[1]);
         }
         // ---- publish T_{k+1} ----
         __threadfence();
         __syncthreads();
         if (tid == 0) st_release_gpu(flags + task, k + 1);
         // ---- per-column partial sums (the halo buffer is free now) ----
-        double *red = reinterpret_cast<double *>(halo);
-        red[(w * kPCols + cl) * 2 + 0] = see[0];
-        red[(w * kPCols + cl) * 2 + 1] = seo[0];
-        red[(w * kPCols + cl + 1) * 2 + 0] = see[1];
-        red[(w * kPCols + cl + 1) * 2 + 1] = seo[1];
+        float *red = halo;  // [warps][64][2 sums][hi, lo]
+        float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)w * kPCols + cl) * 4);
+        rb[0] = make_float4(hs[0], ls[0], hs[1], ls[1]);
+        rb[1] = make_float4(hs[2], ls[2], hs[3], ls[3]);
         __syncthreads();
         if (tid < 2 * kPCols) {
             const int j = tid >> 1, which = tid & 1;
-            double sacc = 0.0;
+            float hsum = 0.f, lsum = 0.f;
 #pragma unroll
-            for (int q = 0; q < kPWarps; q++) sacc += red[(q * kPCols + j) * 2 + which];
-            partial[(((int64_t)k * G + g) * B + col0 + j) * 2 + which] = sacc;
+            for (int q = 0; q < kPWarps; q++) {
+                const float2 v = *reinterpret_cast<const float2 *>(red + ((size_t)q * kPCols + j) * 4 + which * 2);
+                pair_add(hsum, lsum, v.x);
+                lsum += v.y;
+            }
+            partial[(((int64_t)k * G + g) * B + col0 + j) * 2 + which] = make_float2(hsum, lsum);
         }
         __syncthreads();
     }
@@ -848,7 +868,7 @@ int cheb_f32_persistent_setup(int R, size_t smem, int *ctas_per_sm)
 }
 
 int launch_cheb_f32_persistent(cudaStream_t st, const DevMatrix &m, const PersistPlan &pp, int K,
-                               int B, int c0, float *G0, float *G1, double *partial, int *flags,
+                               int B, int c0, float *G0, float *G1, float2 *partial, int *flags,
                                int *err)
 {
     const size_t smem = cheb_f32_persistent_smem(pp.R, pp.maxH, pp.maxBlk, pp.maxNG);
@@ -869,34 +889,6 @@ int launch_cheb_f32_persistent(cudaStream_t st, const DevMatrix &m, const Persis
     default: return (int)cudaErrorInvalidValue;
     }
     return (int)cudaLaunchCooperativeKernel(fn, dim3(G * nc), dim3(32 * kPWarps), args, smem, st);
-}
-
-// Sum the per-rowgroup partials of a slab and turn them into moments:
-// d[2k][j] = 2 <T_k,T_k>_j - 1,  d[2k+1][j] = 2 <T_k,T_{k+1}>_j - X_jj.
-__global__ void k_f32_finalize(const double *__restrict__ partial, int K, int rowgroups, int B,
-                               int c0, int n, const float *__restrict__ xdiag32,
-                               double *__restrict__ d, int M)
-{
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int k = blockIdx.y;
-    if (j >= B || k >= K) return;
-    const int i = c0 + j;
-    if (i >= n) return;
-    double se = 0.0, so = 0.0;
-    const double *p = partial + (int64_t)k * rowgroups * B * 2;
-    for (int g = 0; g < rowgroups; g++) {
-        se += p[((int64_t)g * B + j) * 2 + 0];
-        so += p[((int64_t)g * B + j) * 2 + 1];
-    }
-    if (2 * k <= M) d[(int64_t)(2 * k) * n + i] = 2.0 * se - 1.0;
-    if (2 * k + 1 <= M) d[(int64_t)(2 * k + 1) * n + i] = 2.0 * so - (double)xdiag32[i];
-}
-
-void launch_f32_finalize(cudaStream_t st, const DevMatrix &m, const double *partial, int K,
-                         int rowgroups, int B, int c0, double *d, int M)
-{
-    dim3 grid((B + 127) / 128, K);
-    k_f32_finalize<<<grid, 128, 0, st>>>(partial, K, rowgroups, B, c0, m.n, m.xdiag32, d, M);
 }
 
 // ---------------------------------------------------------------------------
