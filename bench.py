@@ -67,6 +67,9 @@ def allmax(ws, x):
 
 
 STEP_KERNELS = {1: "k_cheb_f32_staged", 2: "k_cheb_f32_persistent", 3: "k_cheb_f32_pipe", 4: "k_cheb_f32_pipe"}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per step launch from one
+# ncu capture of that kernel on the 6x6x6 workload: (step kernel, slab width) -> bytes
+DRAM_TRAFFIC_6X6X6 = {(4, 1024): 215.8e6, (1, 512): 91.2e6}
 
 
 def peaks():
@@ -471,7 +474,9 @@ def main():
         "zero_start_fp32": zero,
         "wall_s_per_step": wall / args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                     "frac": achieved / hbm,
+                     "traffic": DRAM_TRAFFIC_6X6X6.get((rep["step_kernel"], B)) if list(cells) == [6, 6, 6] else None,
+                     "traffic_unit": "DRAM bytes per launch (ncu)", "peak_source": src,
                      "kernel": STEP_KERNELS.get(rep["step_kernel"], "k_cheb_f32"), "launches": int(spmm_l),
                      "avg_launch_us": sum(mom_ms) * 1e3 / max(1, spmm_l),
                      "bytes_per_launch": spmm_b / max(1, spmm_l)},
