@@ -69,7 +69,7 @@ def allmax(ws, x):
 STEP_KERNELS = {1: "k_cheb_f32_staged", 2: "k_cheb_f32_persistent", 3: "k_cheb_f32_pipe", 4: "k_cheb_f32_pipe"}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per step launch from one
 # ncu capture of that kernel on the 6x6x6 workload: (step kernel, slab width) -> bytes
-DRAM_TRAFFIC_6X6X6 = {(4, 1024): 215.8e6, (1, 512): 91.2e6}
+DRAM_TRAFFIC_6X6X6 = {(4, 3456): 829.5e6, (4, 1024): 215.8e6, (1, 512): 91.2e6}
 
 
 def peaks():
@@ -175,7 +175,7 @@ def run_reference(args, ws, rank):
     # SCC iteration count of the oracle on the 2x2x2 cell with the same M, kT, mixer
     small = O.cristobalite(2, 2, 2, sigma_ang=WORKLOAD["sigma_ang"], seed=WORKLOAD["seed"])
     r = O.scc(small, O.kpe_params(M=WORKLOAD["M"], kT=WORKLOAD["kT"], n_elec=small.n_elec,
-                                  nthreads=nth), tol=1e-6, max_iter=100, beta=0.2, history=8)
+                                  nthreads=nth), tol=1e-6, max_iter=100, beta=0.2, history=12)
     vals = []
     for i in range(args.warmup + args.steps):
         cb = cpu_sample(mo, WORKLOAD["M"], nth, r["iters"])

@@ -182,7 +182,8 @@ int ensure_pipe_flags(tb_ctx *ctx, int B)
 
 // Slab-width autotuner (column_block = 0): time kTuneSteps Chebyshev steps of
 // one slab for every candidate kernel/width on this matrix and keep the one
-// with the least time per identity column.  Runs once per matrix, precision
+// with the least estimated time per density evaluation (slab time x slabs, so
+// that a last, mostly padded slab counts).  Runs once per matrix, precision
 // and requested FP32 kernel (req, a StepKind; kKindAuto tries them all); the
 // X used is the unshifted one.
 int autotune(tb_ctx *ctx, int req)
@@ -206,12 +207,33 @@ int autotune(tb_ctx *ctx, int req)
             if (!dup) cands.push_back({kind, Bc});
         }
     };
+    // widths in [lo, hi] (multiples of 64) that split n into equal slabs with
+    // the least padding: B = 64 ceil(ceil(n / s) / 64) over slab counts s
+    auto even_widths = [&](int lo, int hi) {
+        std::vector<std::pair<int64_t, int>> w;  // (padding, -B)
+        for (int ns = std::max(1, (m.n + hi - 1) / hi); ns <= (m.n + lo - 1) / lo; ns++) {
+            const int B = ((m.n + ns - 1) / ns + 63) / 64 * 64;
+            if (B < lo || B > hi) continue;
+            w.push_back({(int64_t)ns * B - m.n, -B});
+        }
+        std::sort(w.begin(), w.end());
+        std::vector<int> out;
+        for (auto &e : w)
+            if ((int)out.size() < 3 && std::find(out.begin(), out.end(), -e.second) == out.end()) out.push_back(-e.second);
+        return out;
+    };
+    // the FP32 partial array holds K * rowgroups * B pairs of 16 bytes: keep it under 4 GiB
+    const int Kp = (ctx->p.M + 2) / 2;
+    auto fits = [&](int B, int groups) { return (double)Kp * groups * B * 16.0 <= 4.0 * 1073741824.0; };
     if (prec == TB_PREC_FP32) {
         if ((req == kKindAuto || req == kKindPersistent) && ctx->pp.R > 0) cands.push_back({kKindPersistent, ctx->pp.B});
         if ((req == kKindAuto || req == kKindPipelined) && ctx->pl.stages > 0 && ctx->pl.coop)
             widths(kKindPipelined, {256, 512, 1024}, 64);
-        if ((req == kKindAuto || req == kKindPipelinedStep) && ctx->pl.stages > 0)
+        if ((req == kKindAuto || req == kKindPipelinedStep) && ctx->pl.stages > 0) {
             widths(kKindPipelinedStep, {512, 1024}, 64);
+            for (int B : even_widths(768, 4096))
+                if (fits(B, ctx->pl.G)) widths(kKindPipelinedStep, {B}, 64);
+        }
         if (req == kKindAuto || req == kKindStaged) widths(kKindStaged, {256, 384, 512}, ctx->sp.R > 0 ? 64 : 128);
     } else {
         widths(kKindStaged, {64, 128, 256}, 64);
@@ -285,9 +307,10 @@ int autotune(tb_ctx *ctx, int req)
             cudaEventElapsedTime(&ms, a, b);
         }
         TB_CUDA(cudaGetLastError());
-        const double per_col = ms / (double)std::min(B, m.n);
-        if (per_col < best) {
-            best = per_col;
+        // estimated moment time of a density evaluation: per-slab time x slabs
+        const double per_density = ms * (double)((m.n + B - 1) / B);
+        if (per_density < best) {
+            best = per_density;
             pick = cd;
         }
         dfree(T0);
