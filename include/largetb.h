@@ -129,7 +129,7 @@ typedef struct tb_report {
 
 typedef struct tb_ctx tb_ctx;
 
-/* Fill *p with defaults (M = 200, Jackson, kT = 0.01, FP64, Anderson 12 / 0.2,
+/* Fill *p with defaults (M = 200, Jackson, kT = 0.01, FP64, Anderson 16 / 0.2,
  * scc_tol = 1e-6, SP2 drop 1e-5 / 40 iterations). */
 int tb_params_init(tb_params *p);
 

@@ -1172,7 +1172,7 @@ int tb_params_init(tb_params *p)
     p->mu_tol = 1e-9;
     p->scc_tol = 1e-6;
     p->scc_max_iter = 100;
-    p->mix_history = 12;
+    p->mix_history = 16;
     p->mix_beta = 0.2;
     p->sp2_drop_tol = 1e-5;
     p->sp2_max_iter = 40;

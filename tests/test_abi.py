@@ -35,7 +35,7 @@ def test_struct_layouts_match():
     import largetb_gb300 as T
     p = T.params()
     assert p.struct_size == C.sizeof(T.TbParams)
-    assert p.M == 200 and p.mix_history == 12 and p.scc_tol == 1e-6
+    assert p.M == 200 and p.mix_history == 16 and p.scc_tol == 1e-6
 
 
 def test_no_device_fails_loudly():

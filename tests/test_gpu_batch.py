@@ -22,7 +22,7 @@ def test_batch_matches_oracle(gpu):
     for i, (c, s, sd) in enumerate(CASES):
         o = O.cristobalite(*c, sigma_ang=s, seed=sd)
         ref = O.scc(o, O.kpe_params(M=M, kT=0.01, n_elec=o.n_elec), tol=1e-6, max_iter=100,
-                    beta=0.2, history=12)
+                    beta=0.2, history=16)
         assert ref["status"] == 0
         assert abs(int(r["iters"][i]) - ref["iters"]) <= 1, (i, r["iters"][i], ref["iters"])
         assert np.abs(r["q"][i] - ref["q"]).max() < 1e-6

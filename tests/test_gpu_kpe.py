@@ -112,7 +112,7 @@ def test_coulomb_shift_reference_triple(gpu, golden):
 def test_scc_matches_oracle(gpu, prec):
     m, o = _pair(2, 2, 2)
     ref = O.scc(o, O.kpe_params(M=200, kT=0.01, n_elec=o.n_elec), tol=1e-6, max_iter=100,
-                beta=0.2, history=8)
+                beta=0.2, history=16)
     assert ref["status"] == 0
     with _ctx(gpu, m, M=200, precision=prec) as c:
         r = c.scc_solve()
@@ -125,7 +125,7 @@ def test_scc_matches_oracle(gpu, prec):
 def test_scc_with_initial_charges(gpu):
     m, o = _pair(1, 1, 2, seed=3)
     p = O.kpe_params(M=100, kT=0.01, n_elec=o.n_elec)
-    ref = O.scc(o, p, tol=1e-6, max_iter=100, beta=0.2, history=8)
+    ref = O.scc(o, p, tol=1e-6, max_iter=100, beta=0.2, history=16)
     with _ctx(gpu, m, M=100) as c:
         r = c.scc_solve(q_init=ref["q"])
         r0 = c.scc_solve()
