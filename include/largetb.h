@@ -100,7 +100,12 @@ typedef struct tb_params {
     int32_t sp2_max_iter;
     int32_t fp32_kernel;   /* enum tb_fp32_kernel */
     double sp2_idem_tol;   /* SP2: stop when ||X^2 - X||_F < sp2_idem_tol */
-    double reserved[6];
+    double bounds_lo;      /* if bounds_hi > bounds_lo: the spectral interval that sets   */
+    double bounds_hi;      /* X = (H - b)/a for tb_density / tb_scc_solve / tb_kpm_dos
+                              instead of Gershgorin, unpadded -- runKPM's refined a, b
+                              (withSP2_deltaH.cpp:1696-1703); the caller vouches that it
+                              holds the spectrum.  Default 0, 0: Gershgorin. */
+    double reserved[4];
 } tb_params;
 
 typedef struct tb_report {

@@ -67,7 +67,9 @@ class TbParams(C.Structure):
         ("sp2_max_iter", C.c_int32),
         ("fp32_kernel", C.c_int32),
         ("sp2_idem_tol", C.c_double),
-        ("reserved", C.c_double * 6),
+        ("bounds_lo", C.c_double),
+        ("bounds_hi", C.c_double),
+        ("reserved", C.c_double * 4),
     ]
 
 

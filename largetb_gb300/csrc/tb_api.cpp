@@ -124,6 +124,8 @@ int check_params(tb_ctx *ctx, const tb_params *p)
         return fail(ctx, TB_ERR_INVALID_ARG, "bad pad / tolerance / iteration cap");
     if (p->mix_history < 0 || p->mix_history > kMaxHistory || !(p->mix_beta > 0))
         return fail(ctx, TB_ERR_INVALID_ARG, "mix_history must be in [0,16], mix_beta > 0");
+    if (!std::isfinite(p->bounds_lo) || !std::isfinite(p->bounds_hi))
+        return fail(ctx, TB_ERR_INVALID_ARG, "spectral bounds not finite");
     if (p->fp32_kernel < TB_FP32_AUTO || p->fp32_kernel > TB_FP32_PIPELINED_STEP)
         return fail(ctx, TB_ERR_INVALID_ARG, "unknown fp32_kernel");
     if (!(p->sp2_drop_tol >= 0) || p->sp2_max_iter < 1 || !(p->sp2_idem_tol >= 0))
@@ -766,7 +768,7 @@ int density_eval(tb_ctx *ctx, bool have_shift)
     cudaStream_t st = ctx->stream;
     const int M = p.M, B = w.B;
     const double *shift = have_shift ? w.shift : nullptr;
-    launch_gershgorin(st, m, shift, p.spectral_pad, p.kT, M, w.nq_cap, w.state);
+    launch_gershgorin(st, m, shift, p.spectral_pad, p.kT, M, w.nq_cap, w.state, p.bounds_lo, p.bounds_hi);
     launch_build_x(st, m, shift, p.precision, w.state);
     ctx->launches += 2;
 

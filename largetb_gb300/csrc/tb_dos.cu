@@ -118,7 +118,7 @@ int run_kpm_dos(tb_ctx *ctx, int nmom, int nr, uint64_t seed, int npts, double *
             gh[k] = ((N - k + 1) * std::cos(kPi * k / (N + 1)) + std::sin(kPi * k / (N + 1)) * cotv) / (N + 1);
         cudaMemcpyAsync(g, gh.data(), sizeof(double) * nmom, cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(mom, 0, sizeof(double) * nmom, st);
-        launch_gershgorin(st, m, nullptr, 0.0, 0.0, 2, 1 << 22, state);
+        launch_gershgorin(st, m, nullptr, 0.0, 0.0, 2, 1 << 22, state, ctx->p.bounds_lo, ctx->p.bounds_hi);
         launch_build_x(st, m, nullptr, TB_PREC_FP64, state);
         int blocks = (int)std::min<int64_t>((tot + 255) / 256, 152 * 8);
         k_probe_init<<<blocks, 256, 0, st>>>(T0, R, m.n, B, nr, seed);

@@ -172,7 +172,8 @@ namespace tb {
 void launch_coulomb_shift(cudaStream_t st, const DevScc &s, const double *q, double *V,
                           double *shift);
 void launch_gershgorin(cudaStream_t st, const DevMatrix &m, const double *shift, double pad,
-                       double kT, int M, int nq_cap, DevState *state);
+                       double kT, int M, int nq_cap, DevState *state, double fix_lo = 0.0,
+                       double fix_hi = 0.0);
 void launch_build_x(cudaStream_t st, const DevMatrix &m, const double *shift, int precision,
                     const DevState *state);
 void launch_slab_identity(cudaStream_t st, void *T0, int n, int B, int c0, int precision);

@@ -14,9 +14,10 @@
 //                       SCC diagonal shift of constructdeltaH 1443-1459
 //   k_cheb_f64          getKPE recurrence 1134-1168 on identity column slabs with
 //                       the unit-vector diagonal extraction of 1361-1379
-//   k_cheb_f32          same recurrence in FP32 to order M/2; moments from
+//   k_cheb_f32*         same recurrence in FP32 to order M/2; moments from
 //                       T_{2k} = 2 T_k^2 - I and T_{2k+1} = 2 T_k T_{k+1} - X
-//                       (FP64-accumulated column dot products)
+//                       (column dot products as FP32 TwoSum pairs; the
+//                       pipelined form is in tb_pipe.cu)
 //   k_moment_sums ..    tr T_k, damped DOS, mu bisection: runKPM 1579-1712
 //   k_fermi_coeffs      getKPE coefficients 1100-1103 (Fermi instead of step)
 //   k_charges           computeDiagonalElements 1375-1385 (diagP, orbital2Atom)
@@ -113,13 +114,15 @@ void launch_coulomb_shift(cudaStream_t st, const DevScc &s, const double *q, dou
 }
 
 // ---------------------------------------------------------------------------
-// Gershgorin bounds of H0 + diag(shift) and the scaling X = (H - b)/a.
+// Gershgorin bounds of H0 + diag(shift) and the scaling X = (H - b)/a; with
+// fix_hi > fix_lo the caller's interval [fix_lo, fix_hi] sets a and b instead
+// (runKPM's refined a, b of withSP2_deltaH.cpp:1696-1703), unpadded.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_gershgorin(int n, const double *__restrict__ h0diag,
                                                      const double *__restrict__ radius,
                                                      const double *__restrict__ shift,
                                                      double pad, double kT, int M, int nq_cap,
-                                                     DevState *st)
+                                                     double fix_lo, double fix_hi, DevState *st)
 {
     __shared__ double smin[32], smax[32];
     double mn = INFINITY, mx = -INFINITY;
@@ -145,10 +148,11 @@ __global__ void __launch_bounds__(1024) k_gershgorin(int n, const double *__rest
         if (lane == 0) {
             st->lmin = mn;
             st->lmax = mx;
-            const double half = 0.5 * (mx - mn);
-            const double a = half * (1.0 + pad);
+            const bool fixed = fix_hi > fix_lo;
+            const double half = fixed ? 0.5 * (fix_hi - fix_lo) : 0.5 * (mx - mn);
+            const double a = fixed ? half : half * (1.0 + pad);
             st->a = a;
-            st->b = 0.5 * (mx + mn);
+            st->b = fixed ? 0.5 * (fix_hi + fix_lo) : 0.5 * (mx + mn);
             st->status = (a > 0 && isfinite(a)) ? 0 : TB_ERR_SPECTRUM;
             st->beta_x = kT > 0 ? a / kT : 0.0;
             // quadrature size rule shared with the oracle: next power of two
@@ -171,9 +175,10 @@ __global__ void __launch_bounds__(1024) k_gershgorin(int n, const double *__rest
 }
 
 void launch_gershgorin(cudaStream_t st, const DevMatrix &m, const double *shift, double pad,
-                            double kT, int M, int nq_cap, DevState *state)
+                            double kT, int M, int nq_cap, DevState *state, double fix_lo, double fix_hi)
 {
-    k_gershgorin<<<1, 1024, 0, st>>>(m.n, m.h0diag, m.radius, shift, pad, kT, M, nq_cap, state);
+    k_gershgorin<<<1, 1024, 0, st>>>(m.n, m.h0diag, m.radius, shift, pad, kT, M, nq_cap, fix_lo, fix_hi,
+                                     state);
 }
 
 // ---------------------------------------------------------------------------

@@ -17,12 +17,17 @@
  *     orbit2Atom.m;
  *   - the Coulomb shift against the netCharge.m -> GammaQ_vector.m -> deltaH.m
  *     triple of one reference run;
- *   - the closed-form Jackson damping against column 1 of gnsfile.txt.
- * What no reference output pins (every reference run seeds its random vectors
- * from std::random_device): the exact-trace moments, mu, diagP, charges, the
- * SCC loop and SP2 results.  Those are "parity unpinned" by reference data and
- * are checked instead against dense eigendecomposition (numpy) and the
- * kT -> 0 limit of the reference's step coefficients.
+ *   - the closed-form Jackson damping against column 1 of gnsfile.txt;
+ *   - statistically, the Chebyshev moment recurrence: the exact traces
+ *     tr T_k((H - b)/a) of the reference's Htotal_scc.m (symmetrised as
+ *     runKPM does) at the reference's own a, b match the moments behind its
+ *     20-vector DOS dosfile.txt to sampling noise (|z| < 2 over 400 moments;
+ *     a different matrix scores mean z^2 ~ 2700).
+ * What no reference output pins exactly (every reference run seeds its random
+ * vectors from std::random_device): the exact-trace moments beyond that
+ * statistical agreement, mu, diagP, charges, the SCC loop and SP2 results.
+ * Those are checked against dense eigendecomposition (numpy) and the kT -> 0
+ * limit of the reference's step coefficients.
  *
  * Units: bohr, Hartree, electrons.  Orbital order per atom: s, px, py, pz.
  */

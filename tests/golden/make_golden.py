@@ -13,6 +13,9 @@ tests/golden/reference_dumps.npz:
   netcharge         netCharge.m    delta q of that step (576)
   gammaq            GammaQ_vector.m  Gamma * delta q (576)
   gns_col1          gnsfile.txt column 1: Jackson g_n, N = 1000 (6-digit print)
+  hscc_{r,c,v}      Htotal_scc.m  H of one SCC iteration (2304 x 2304)
+  dosfile           dosfile.txt   runKPM's DOS of Htotal_scc: 2000 x (energy, dos),
+                    N = 1000 Jackson moments from 20 Gaussian vectors, printed %lf
 
 Indices are 0-based.  Run once where the reference is mounted; the tests use
 only the .npz, never the reference tree.
@@ -64,7 +67,7 @@ def main(ref="/root/reference", out=None):
     out = out or os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_dumps.npz")
     d = {}
     for key, name in [("amat", "Amat.m"), ("h444", "H.m"), ("gamma", "GAMMA_AB.m"),
-                      ("o2a", "orbit2Atom.m"), ("dh", "deltaH.m")]:
+                      ("o2a", "orbit2Atom.m"), ("dh", "deltaH.m"), ("hscc", "Htotal_scc.m")]:
         r, c, v, shape = read_mat(os.path.join(ref, name))
         d[key + "_r"], d[key + "_c"], d[key + "_v"] = r, c, v
         d[key + "_shape"] = np.array(shape, np.int32)
@@ -72,6 +75,7 @@ def main(ref="/root/reference", out=None):
     d["gammaq"] = read_vec(os.path.join(ref, "GammaQ_vector.m"))
     gns = np.loadtxt(os.path.join(ref, "gnsfile.txt"))
     d["gns_col1"] = gns[:, 0]
+    d["dosfile"] = np.loadtxt(os.path.join(ref, "dosfile.txt"), delimiter=",")
     np.savez_compressed(out, **d)
     print("wrote", out, {k: v.shape for k, v in d.items()})
 

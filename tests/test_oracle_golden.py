@@ -154,3 +154,21 @@ def test_product_builder_matches_oracle():
     q = T.model_quartz(2, 2, 1)
     oq = O.quartz(2, 2, 1)
     np.testing.assert_allclose(q.vals, oq.val, atol=1e-14, rtol=0)
+
+
+def test_moments_pinned_by_reference_dos(golden):
+    """Statistical pin of the KPE recurrence on a reference matrix: the
+    oracle's exact traces tr T_k((H - b)/a) of Htotal_scc, at the reference's
+    own a, b, against the moments behind the reference's 20-vector DOS
+    (dosfile.txt).  A different matrix (H.m) scores mean z^2 in the
+    thousands."""
+    from tests.conftest import moment_z, reference_dos
+    H, a, b, mu, nvec = reference_dos(golden)
+    n = H.shape[0]
+    assert abs(nvec - 20) < 1.5  # runKPM's nRandoms
+    m = O.model_from_csr(H.indptr, H.indices, H.data, n // 4)
+    K = 120
+    tr = O.exact_moments(m, a, b, 2 * K + 1).sum(1)
+    assert abs(tr[0] - n) < 1e-9
+    z = moment_z(mu, nvec, tr, n, K)[1:]
+    assert np.abs(z).max() < 5 and np.mean(z ** 2) < 2
