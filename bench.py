@@ -305,7 +305,9 @@ def run_sp2_bench(args, T, dev, rank):
             r = c.sp2()
             ts.append(r["report"]["t_total_ms"] / 1e3)
         rep = r["report"]
-        out[name] = {"s_per_solve": statistics.mean(ts), "iters": rep["sp2_iters"],
+        t = statistics.mean(ts)
+        out[name] = {"s_per_solve": t, "iters": rep["sp2_iters"],
+                     "gflops": rep["sp2_flops"] / t / 1e9, "GBps_algorithmic": rep["sp2_bytes"] / t / 1e9,
                      "idem_err": rep["idem_err"], "nnzb": rep["sp2_nnzb"],
                      "blocks_per_row": rep["sp2_nnzb"] / m.natoms, "e_band": r["e_band"],
                      "q_sum": float(r["q"].sum())}

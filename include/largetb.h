@@ -129,7 +129,9 @@ typedef struct tb_report {
     int32_t sp2_iters;
     int32_t step_kernel;      /* FP32 form: enum tb_fp32_kernel actually used */
     int64_t sp2_nnzb;         /* SP2: stored blocks of the returned X */
-    double reserved[8];
+    double sp2_flops;         /* SP2: 128 x (4x4 block products) over all steps */
+    double sp2_bytes;         /* SP2: algorithmic bytes, every X_k read once and X_{k+1} written once */
+    double reserved[6];
 } tb_report;
 
 typedef struct tb_ctx tb_ctx;

@@ -97,7 +97,9 @@ class TbReport(C.Structure):
         ("sp2_iters", C.c_int32),
         ("step_kernel", C.c_int32),
         ("sp2_nnzb", C.c_int64),
-        ("reserved", C.c_double * 8),
+        ("sp2_flops", C.c_double),
+        ("sp2_bytes", C.c_double),
+        ("reserved", C.c_double * 6),
     ]
 
     def as_dict(self):

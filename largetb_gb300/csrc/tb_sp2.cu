@@ -32,6 +32,7 @@ struct Sp2Scalars {
     double trX2, idem2, trNew, trX;
     unsigned long long count;
     unsigned long long bound;
+    unsigned long long products;  // 4x4 block products of the step (64 FMA each)
     int overflow;
     int pad;
 };
@@ -121,19 +122,27 @@ __global__ void k_sp2_init(int nb, const int32_t *__restrict__ rowptr,
     if ((threadIdx.x & 31) == 0 && tr != 0.0) atomicAdd(&sc->trX, tr);
 }
 
-// Upper bound of the blocks of X^2: sum_I min(nb, sum_{K in row I} len(K)).
+// Upper bound of the blocks of X^2: sum_I min(nb, sum_{K in row I} len(K));
+// the uncapped sum is the number of block products of the step.
 __global__ void k_sp2_bound(int nb, const int32_t *__restrict__ rs, const int32_t *__restrict__ rl,
                             const int32_t *__restrict__ col, Sp2Scalars *sc)
 {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned long long b = 0;
+    unsigned long long b = 0, p = 0;
     if (I < nb) {
         long long s = 0;
         for (int t = 0; t < rl[I]; t++) s += rl[col[rs[I] + t]];
         b = (unsigned long long)(s < nb ? s : nb);
+        p = (unsigned long long)s;
     }
-    for (int o = 16; o > 0; o >>= 1) b += __shfl_xor_sync(0xffffffffu, b, o);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&sc->bound, b);
+    for (int o = 16; o > 0; o >>= 1) {
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+        p += __shfl_xor_sync(0xffffffffu, p, o);
+    }
+    if ((threadIdx.x & 31) == 0 && b) {
+        atomicAdd(&sc->bound, b);
+        atomicAdd(&sc->products, p);
+    }
 }
 
 template <typename T>
@@ -370,6 +379,8 @@ int sp2_run(tb_ctx *ctx, double *diagP_h, double *q_h, double *e_band, tb_report
     cudaError_t e;
     Sp2Scalars hs;
     int64_t launches = 0;
+    double products = 0.0, moved = 0.0;  // block products and algorithmic bytes over all steps
+    int64_t cur_nnzb = 0;
     int it = 0;
     double idem = INFINITY, prev1 = INFINITY, prev2 = INFINITY, trX = 0.0;
     // shared-memory budget of k_sp2_step
@@ -428,6 +439,7 @@ int sp2_run(tb_ctx *ctx, double *diagP_h, double *q_h, double *e_band, tb_report
         }
     }
     trX = hs.trX;
+    cur_nnzb = m.nnzb;
     for (it = 0;; it++) {
         // capacity of X^2
         cudaMemsetAsync(sc, 0, sizeof(Sp2Scalars), st);
@@ -441,6 +453,7 @@ int sp2_run(tb_ctx *ctx, double *diagP_h, double *q_h, double *e_band, tb_report
             cuda_fail(e, "cudaMalloc(sp2 X^2)");
             goto done;
         }
+        products += (double)hs.products;
         const int branch = (2.0 * trX > ne) ? -1 : 1;  // withSP2.cpp:1029-1030
         k_sp2_step<T><<<grid, kSp2Threads, smem, st>>>(nb, A.rs, A.rl, A.col, (const T *)A.blk, branch, drop2,
                                                        B.rs, B.rl, B.col, (T *)B.blk, B.cap, sc, gacc,
@@ -457,6 +470,8 @@ int sp2_run(tb_ctx *ctx, double *diagP_h, double *q_h, double *e_band, tb_report
             goto done;
         }
         idem = std::sqrt(hs.idem2);
+        // algorithmic bytes of the step: X_k blocks + columns read once, X_{k+1} written once
+        moved += (double)(cur_nnzb + (int64_t)hs.count) * (16.0 * sizeof(T) + 4.0) + 16.0 * nb;
         bool stop = false;
         if (idem < ctx->p.sp2_idem_tol) stop = true;
         // stagnation once in the quadratic regime (the oracle's rule)
@@ -465,6 +480,7 @@ int sp2_run(tb_ctx *ctx, double *diagP_h, double *q_h, double *e_band, tb_report
         if (stop) break;
         branches.push_back(branch);
         std::swap(A, B);
+        cur_nnzb = (int64_t)hs.count;
         trX = hs.trNew;
         prev2 = prev1;
         prev1 = idem;
@@ -496,6 +512,8 @@ int sp2_run(tb_ctx *ctx, double *diagP_h, double *q_h, double *e_band, tb_report
             rep->idem_err = idem;
             rep->sp2_iters = it;
             rep->sp2_nnzb = nnzb;
+            rep->sp2_flops = 128.0 * products;
+            rep->sp2_bytes = moved;
             rep->kernel_launches = launches;
             rep->precision = ctx->p.precision;
         }
