@@ -67,10 +67,28 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total)
     return before;
 }
 
+// (s, c) += x with the rounding error of s + x kept exactly in c (TwoSum)
+__device__ __forceinline__ void pair_add(float &s, float &c, float x)
+{
+    const float t = s + x;
+    const float bp = t - s;
+    const float e = (s - (t - bp)) + (x - bp);
+    s = t;
+    c += e;
+}
+
 __device__ __forceinline__ double warp_sum_d(double v)
 {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+// Element (m, s) of the 4x4 block whose element (r, s) this lane holds, from
+// lane 4 m + s of the same half warp.
+template <typename T>
+__device__ __forceinline__ T col_of(T e, int s, int m)
+{
+    return __shfl_sync(0xffffffffu, e, 4 * m + s, 16);
 }
 
 template <typename T>
@@ -169,20 +187,50 @@ __global__ void __launch_bounds__(kSp2Threads)
     for (size_t i = tid; i < (size_t)nb * 16; i += kSp2Threads) acc[i] = T(0);
     __syncthreads();
     double trX2 = 0.0, idem2 = 0.0, trNew = 0.0;
+    float ih = 0.f, il = 0.f;  // FP32 blocks: sum of (X^2 - X)^2 as a TwoSum pair
     for (int I = blockIdx.x; I < nb; I += gridDim.x) {
         const int ri = rs[I], li = rl[I];
         // ---- phase A: row I of X^2 ----
+        // a half warp forms one 4x4 block product: lane (r, s) loads element
+        // (r, s) of B (one coalesced 64-byte load per block), gathers column s
+        // by shuffles and accumulates its entry of A B into the dense row;
+        // four products per half warp have their loads in flight together.
         for (int t = w; t < li; t += kSp2Threads / 32) {
             const int K = col[ri + t];
             const T *A = blk + (size_t)(ri + t) * 16;
             const T a0 = A[4 * r + 0], a1 = A[4 * r + 1], a2 = A[4 * r + 2], a3 = A[4 * r + 3];
             const int rk = rs[K], lk = rl[K];
-            for (int u = half; u < lk; u += 2) {
-                const int J = col[rk + u];
-                const T *Bm = blk + (size_t)(rk + u) * 16;
-                const T v = a0 * Bm[s] + a1 * Bm[4 + s] + a2 * Bm[8 + s] + a3 * Bm[12 + s];
-                atomicAdd(acc + (size_t)J * 16 + l16, v);
-                if (l16 == 0) atomicOr(bm + (J >> 5), 1u << (J & 31));
+            // warp-uniform trip counts (base is the same in both half warps),
+            // so the 16-lane shuffles always run converged
+            int base = 0;
+            for (; base + 7 < lk; base += 8) {
+                const int u = base + half;
+                int J[4];
+                T e[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    J[j] = col[rk + u + 2 * j];
+                    e[j] = blk[(size_t)(rk + u + 2 * j) * 16 + l16];
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const T v = a0 * col_of(e[j], s, 0) + a1 * col_of(e[j], s, 1) + a2 * col_of(e[j], s, 2) +
+                                a3 * col_of(e[j], s, 3);
+                    atomicAdd(acc + (size_t)J[j] * 16 + l16, v);
+                    if (l16 == 0) atomicOr(bm + (J[j] >> 5), 1u << (J[j] & 31));
+                }
+            }
+            // remainder: the missing products of the last pair are masked
+            for (; base < lk; base += 2) {
+                const int uu = base + half;
+                const bool ok = uu < lk;
+                const int J = ok ? col[rk + uu] : 0;
+                const T e = ok ? blk[(size_t)(rk + uu) * 16 + l16] : T(0);
+                const T v = a0 * col_of(e, s, 0) + a1 * col_of(e, s, 1) + a2 * col_of(e, s, 2) + a3 * col_of(e, s, 3);
+                if (ok) {
+                    atomicAdd(acc + (size_t)J * 16 + l16, v);
+                    if (l16 == 0) atomicOr(bm + (J >> 5), 1u << (J & 31));
+                }
             }
         }
         __syncthreads();
@@ -219,9 +267,18 @@ __global__ void __launch_bounds__(kSp2Threads)
             const int xi = valid ? find_col<T>(col, ri, li, J) : -1;
             const T xo = xi >= 0 ? blk[(size_t)xi * 16 + l16] : T(0);
             const T nv = branch < 0 ? x2 : T(2) * xo - x2;
-            const double dl = (double)x2 - (double)xo;
-            idem2 += dl * dl;
-            float nrm = (float)((double)nv * (double)nv);
+            float nrm;
+            if constexpr (sizeof(T) == 4) {
+                // FP32 blocks: FP32 norms (GB300 issues FP64 at ~1/64 the rate);
+                // the idempotency sum is a TwoSum pair
+                const float dl = x2 - xo;
+                pair_add(ih, il, dl * dl);
+                nrm = nv * nv;
+            } else {
+                const double dl = (double)x2 - (double)xo;
+                idem2 += dl * dl;
+                nrm = (float)((double)nv * (double)nv);
+            }
             for (int o = 8; o > 0; o >>= 1) nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
             const int kp = (double)nrm >= drop2;
             if (valid) {
@@ -275,6 +332,7 @@ __global__ void __launch_bounds__(kSp2Threads)
         }
         __syncthreads();
     }
+    idem2 += (double)ih + (double)il;
     trX2 = warp_sum_d(trX2);
     idem2 = warp_sum_d(idem2);
     trNew = warp_sum_d(trNew);
