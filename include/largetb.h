@@ -54,8 +54,9 @@ enum tb_status {
 
 enum tb_precision {
     TB_PREC_FP64 = 0, /* plain form: FP64 recurrence, T_{k+1} = 2 X T_k - T_{k-1} */
-    TB_PREC_FP32 = 1  /* FP32 recurrence to order M/2 with FP64-accumulated moments
-                         from T_{2k} = 2 T_k^2 - 1, T_{2k+1} = 2 T_k T_{k+1} - X */
+    TB_PREC_FP32 = 1  /* FP32 recurrence to order M/2; moments from T_{2k} = 2 T_k^2 - 1,
+                         T_{2k+1} = 2 T_k T_{k+1} - X, the column dot products summed as
+                         FP32 TwoSum pairs (~44 bits) and returned in FP64 */
 };
 
 /* Chebyshev step kernel of the FP32 form (tb_params.fp32_kernel).  No
