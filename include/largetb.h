@@ -71,6 +71,15 @@ enum tb_fp32_kernel {
     TB_FP32_PIPELINED_STEP = 4 /* the same kernel, one launch per step */
 };
 
+/* Density-matrix solver of tb_density (tb_params.mode): the reference's two
+ * programs, withSP2_deltaH.cpp (KPE) and withSP2.cpp (SP2). */
+enum tb_mode {
+    TB_MODE_KPE = 0, /* kernel polynomial expansion (runKPM + computeDensityMatrix) */
+    TB_MODE_SP2 = 1  /* SP2 purification (getSP2 / computeAlphas); tb_density then
+                        leaves mu and moments untouched, and tb_scc_solve answers
+                        TB_ERR_UNSUPPORTED: the reference's SCC program is KPE only */
+};
+
 enum tb_kernel_kind {
     TB_KERNEL_JACKSON = 0,  /* closed form of runKPM, withSP2_deltaH.cpp:1593-1595 */
     TB_KERNEL_AUTOCORR = 1, /* getKPE's autocorrelation form, withSP2_deltaH.cpp:1104-1132 */
@@ -106,7 +115,9 @@ typedef struct tb_params {
                               instead of Gershgorin, unpadded -- runKPM's refined a, b
                               (withSP2_deltaH.cpp:1696-1703); the caller vouches that it
                               holds the spectrum.  Default 0, 0: Gershgorin. */
-    double reserved[4];
+    int32_t mode;          /* enum tb_mode */
+    int32_t reserved_i;
+    double reserved[3];
 } tb_params;
 
 typedef struct tb_report {

@@ -45,6 +45,8 @@ FP32_STAGED = 1
 FP32_PERSISTENT = 2
 FP32_PIPELINED = 3
 FP32_PIPELINED_STEP = 4
+MODE_KPE = 0
+MODE_SP2 = 1
 
 
 class TbParams(C.Structure):
@@ -69,7 +71,9 @@ class TbParams(C.Structure):
         ("sp2_idem_tol", C.c_double),
         ("bounds_lo", C.c_double),
         ("bounds_hi", C.c_double),
-        ("reserved", C.c_double * 4),
+        ("mode", C.c_int32),
+        ("reserved_i", C.c_int32),
+        ("reserved", C.c_double * 3),
     ]
 
 

@@ -124,6 +124,7 @@ int check_params(tb_ctx *ctx, const tb_params *p)
         return fail(ctx, TB_ERR_INVALID_ARG, "bad pad / tolerance / iteration cap");
     if (p->mix_history < 0 || p->mix_history > kMaxHistory || !(p->mix_beta > 0))
         return fail(ctx, TB_ERR_INVALID_ARG, "mix_history must be in [0,16], mix_beta > 0");
+    if (p->mode != TB_MODE_KPE && p->mode != TB_MODE_SP2) return fail(ctx, TB_ERR_INVALID_ARG, "unknown mode");
     if (!std::isfinite(p->bounds_lo) || !std::isfinite(p->bounds_hi))
         return fail(ctx, TB_ERR_INVALID_ARG, "spectral bounds not finite");
     if (p->fp32_kernel < TB_FP32_AUTO || p->fp32_kernel > TB_FP32_PIPELINED_STEP)
@@ -1410,6 +1411,10 @@ int tb_density(tb_ctx *ctx, const double *shift, double *diagP, double *q, doubl
     if (shift)
         for (int i = 0; i < ctx->m.n; i++)
             if (!std::isfinite(shift[i])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in shift");
+    if (ctx->p.mode == TB_MODE_SP2) {
+        if (shift) return fail(ctx, TB_ERR_UNSUPPORTED, "SP2 mode takes no diagonal shift");
+        return tb_sp2(ctx, diagP, q, e_band, rep);
+    }
     TB_TRY(set_device(ctx));
     TB_TRY(ensure_work(ctx));
     cudaEvent_t e0;
@@ -1454,6 +1459,8 @@ int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, do
     if (!ctx) return TB_ERR_INVALID_ARG;
     if (!ctx->have_h || !ctx->have_scc)
         return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian and SCC data must be set");
+    if (ctx->p.mode != TB_MODE_KPE)
+        return fail(ctx, TB_ERR_UNSUPPORTED, "the SCC loop runs on the KPE solver only (as the reference's)");
     const size_t n = ctx->m.n, na = ctx->m.natoms;
     if (q_init)
         for (size_t a = 0; a < na; a++)

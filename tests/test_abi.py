@@ -61,6 +61,8 @@ def test_bad_params_rejected_before_device():
     assert L.tb_ctx_create(C.byref(p), C.byref(h)) == T.api.TB_ERR_INVALID_ARG
     p = T.params(fp32_kernel=5)
     assert L.tb_ctx_create(C.byref(p), C.byref(h)) == T.api.TB_ERR_INVALID_ARG
+    p = T.params(mode=2)
+    assert L.tb_ctx_create(C.byref(p), C.byref(h)) == T.api.TB_ERR_INVALID_ARG
     p = T.params()
     p.struct_size = 8
     assert L.tb_ctx_create(C.byref(p), C.byref(h)) == T.api.TB_ERR_INVALID_ARG

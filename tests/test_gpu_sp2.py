@@ -65,3 +65,20 @@ def test_sp2_full_size_4x4x4(gpu):
     for r in (r64, r32):
         assert abs(r["q"].sum() - m.n_electrons) < 1e-2
         assert r["report"]["idem_err"] < 1e-2
+
+
+def test_density_in_sp2_mode_is_sp2(gpu):
+    """tb_params.mode = SP2 routes tb_density to the SP2 solver (same result as
+    tb_sp2); the SCC loop stays KPE-only and says so."""
+    m = gpu.model_cristobalite(2, 2, 2, sigma_ang=0.08, seed=3003)
+    with gpu.Context(precision=gpu.PREC_FP64) as c:
+        c.set_model(m)
+        ref = c.sp2()
+        c.set_params(mode=gpu.MODE_SP2)
+        r = c.density()
+        # the row accumulator adds with shared-memory atomics: equal to round-off
+        np.testing.assert_allclose(r["q"], ref["q"], atol=1e-9, rtol=0)
+        assert abs(r["e_band"] - ref["e_band"]) < 1e-9 * m.natoms
+        with pytest.raises(gpu.TbError) as e:
+            c.scc_solve()
+        assert e.value.status == gpu.api.TB_ERR_UNSUPPORTED
