@@ -116,7 +116,9 @@ typedef struct tb_params {
                               (withSP2_deltaH.cpp:1696-1703); the caller vouches that it
                               holds the spectrum.  Default 0, 0: Gershgorin. */
     int32_t mode;          /* enum tb_mode */
-    int32_t reserved_i;
+    int32_t check_fp32;    /* FP32 form: tb_density also runs the plain FP64 recurrence on
+                              the first 64 identity columns (same a, b) and reports the
+                              largest diagP difference there (tb_report.fp32_diag_err) */
     double reserved[3];
 } tb_params;
 
@@ -143,7 +145,10 @@ typedef struct tb_report {
     int64_t sp2_nnzb;         /* SP2: stored blocks of the returned X */
     double sp2_flops;         /* SP2: 128 x (4x4 block products) over all steps */
     double sp2_bytes;         /* SP2: algorithmic bytes, every X_k read once and X_{k+1} written once */
-    double reserved[6];
+    double fp32_diag_err;     /* with check_fp32: max |diagP(FP32) - diagP(FP64)| over the
+                                 checked orbitals, else 0 */
+    double fp32_check_ms;     /* CUDA-event time of that check */
+    double reserved[4];
 } tb_report;
 
 typedef struct tb_ctx tb_ctx;

@@ -72,7 +72,7 @@ class TbParams(C.Structure):
         ("bounds_lo", C.c_double),
         ("bounds_hi", C.c_double),
         ("mode", C.c_int32),
-        ("reserved_i", C.c_int32),
+        ("check_fp32", C.c_int32),
         ("reserved", C.c_double * 3),
     ]
 
@@ -103,7 +103,9 @@ class TbReport(C.Structure):
         ("sp2_nnzb", C.c_int64),
         ("sp2_flops", C.c_double),
         ("sp2_bytes", C.c_double),
-        ("reserved", C.c_double * 6),
+        ("fp32_diag_err", C.c_double),
+        ("fp32_check_ms", C.c_double),
+        ("reserved", C.c_double * 4),
     ]
 
     def as_dict(self):

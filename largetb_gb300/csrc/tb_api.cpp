@@ -861,6 +861,68 @@ int density_eval(tb_ctx *ctx, bool have_shift)
     return TB_OK;
 }
 
+// FP32-form check: the plain FP64 recurrence on the first min(64, n) identity
+// columns with the a, b of the evaluation just run (the FP64 X is rebuilt from
+// the same device state); moments into chk_d[(M+1)][n].
+int fp32_check_slab(tb_ctx *ctx, bool have_shift, float *ms)
+{
+    DevMatrix &m = ctx->m;
+    const int M = ctx->p.M;
+    cudaStream_t st = ctx->stream;
+    if (ctx->chk_M != M || !ctx->chk_d) {
+        dfree(ctx->chk_T0);
+        dfree(ctx->chk_T1);
+        dfree(ctx->chk_d);
+        ctx->chk_M = 0;
+        TB_TRY(dalloc(ctx, ctx->chk_T0, (size_t)m.n * 64));
+        TB_TRY(dalloc(ctx, ctx->chk_T1, (size_t)m.n * 64));
+        TB_TRY(dalloc(ctx, ctx->chk_d, (size_t)(M + 1) * m.n));
+        ctx->chk_M = M;
+    }
+    if (!m.x64) TB_TRY(dalloc(ctx, m.x64, (size_t)m.nnzb * 16));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    launch_build_x(st, m, have_shift ? ctx->w.shift : nullptr, TB_PREC_FP64, ctx->w.state);
+    launch_slab_identity(st, ctx->chk_T0, m.n, 64, 0, TB_PREC_FP64);
+    for (int kout = 1; kout <= M; kout++) {
+        const bool odd = kout & 1;
+        launch_cheb_step_f64(st, m, odd ? ctx->chk_T0 : ctx->chk_T1, odd ? ctx->chk_T1 : ctx->chk_T0, 64, 0,
+                             kout == 1, ctx->chk_d, kout);
+    }
+    cudaEventRecord(e1, st);
+    const cudaError_t e = cudaEventSynchronize(e1);
+    cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    TB_CUDA(e);
+    ctx->launches += 2 + M + 1;
+    return TB_OK;
+}
+
+// max over the checked orbitals of |sum_k c_k g_k (d32[k][i] - d64[k][i])|
+int fp32_check_compare(tb_ctx *ctx, double *err)
+{
+    const int M = ctx->p.M, n = ctx->m.n, cols = std::min(64, n);
+    std::vector<double> d32((size_t)M * cols), d64((size_t)M * cols), c(M), g(M);
+    TB_CUDA(cudaMemcpy2DAsync(d32.data(), cols * 8, ctx->w.d, (size_t)n * 8, cols * 8, M, cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    TB_CUDA(cudaMemcpy2DAsync(d64.data(), cols * 8, ctx->chk_d, (size_t)n * 8, cols * 8, M, cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    TB_CUDA(cudaMemcpyAsync(c.data(), ctx->w.c, M * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    TB_CUDA(cudaMemcpyAsync(g.data(), ctx->w.g, M * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    double e = 0.0;
+    for (int i = 0; i < cols; i++) {
+        double s = 0.0;
+        for (int k = 0; k < M; k++) s += c[k] * g[k] * (d32[(size_t)k * cols + i] - d64[(size_t)k * cols + i]);
+        e = std::max(e, std::fabs(s));
+    }
+    *err = e;
+    return TB_OK;
+}
+
 int read_state(tb_ctx *ctx, DevState &hs)
 {
     TB_CUDA(cudaMemcpyAsync(&hs, ctx->w.state, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
@@ -963,6 +1025,10 @@ void free_all(tb_ctx *ctx)
     dfree(w.q);
     dfree(w.partial);
     dfree(w.state);
+    dfree(ctx->chk_T0);
+    dfree(ctx->chk_T1);
+    dfree(ctx->chk_d);
+    ctx->chk_M = 0;
     {
         char *t0 = (char *)w.T0, *t1 = (char *)w.T1;
         dfree(t0);
@@ -1426,6 +1492,13 @@ int tb_density(tb_ctx *ctx, const double *shift, double *diagP, double *q, doubl
     DevState hs;
     TB_TRY(read_state(ctx, hs));
     int rc = state_status(ctx, hs);
+    const bool check = ctx->p.check_fp32 && ctx->p.precision == TB_PREC_FP32 && rc == TB_OK;
+    double chk_err = 0.0;
+    float chk_ms = 0.f;
+    if (check) {
+        TB_TRY(fp32_check_slab(ctx, shift != nullptr, &chk_ms));
+        TB_TRY(fp32_check_compare(ctx, &chk_err));
+    }
     const size_t n = ctx->m.n, na = ctx->m.natoms;
     if (diagP) TB_CUDA(cudaMemcpyAsync(diagP, ctx->w.diagP, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
     if (q) TB_CUDA(cudaMemcpyAsync(q, ctx->w.q, na * 8, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1436,6 +1509,10 @@ int tb_density(tb_ctx *ctx, const double *shift, double *diagP, double *q, doubl
     if (e_band) *e_band = hs.e_band;
     if (mu) *mu = hs.mu;
     fill_report(ctx, e0, hs, 1, rep);
+    if (rep) {
+        rep->fp32_diag_err = chk_err;
+        rep->fp32_check_ms = chk_ms;
+    }
     return rc;
 }
 

@@ -162,6 +162,9 @@ struct tb_ctx {
     int tuned_kind[2][tb::kNumKinds] = {};
     int tuned_B[2][tb::kNumKinds] = {};
     // SP2 device scratch (lazily sized)
+    // FP32-vs-FP64 check of tb_density (tb_params.check_fp32): a 64-column FP64 slab
+    double *chk_T0 = nullptr, *chk_T1 = nullptr, *chk_d = nullptr;
+    int chk_M = 0;
     void *sp2_scratch = nullptr;
     size_t sp2_scratch_bytes = 0;
 };

@@ -283,3 +283,19 @@ def test_autotuner_reports_a_kernel(gpu):
         again = c.density()["report"]
     assert rep["step_kernel"] in (1, 2, 3, 4)
     assert (again["step_kernel"], again["column_block"]) == (rep["step_kernel"], rep["column_block"])
+
+
+def test_fp32_check_reports_recurrence_error(gpu, cfg1):
+    """check_fp32: tb_density reruns 64 identity columns in the plain FP64
+    form at the same a, b and reports the largest diagP difference there --
+    the FP32 recurrence error alone (same mu and coefficients for both)."""
+    m, o, ref = cfg1
+    with _ctx(gpu, m, M=200, precision=gpu.PREC_FP32, check_fp32=1) as c:
+        r = c.density()
+    rep = r["report"]
+    assert 0 < rep["fp32_diag_err"] < 1e-6
+    assert rep["fp32_check_ms"] > 0
+    # the FP32 diagP of those orbitals against the oracle's FP64 ones: same order
+    assert np.abs(r["diagP"][:64] - ref["diagP"][:64]).max() < 1e-6
+    with _ctx(gpu, m, M=200, precision=gpu.PREC_FP32) as c:
+        assert c.density()["report"]["fp32_diag_err"] == 0.0
