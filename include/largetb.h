@@ -119,7 +119,11 @@ typedef struct tb_params {
     int32_t check_fp32;    /* FP32 form: tb_density also runs the plain FP64 recurrence on
                               the first 64 identity columns (same a, b) and reports the
                               largest diagP difference there (tb_report.fp32_diag_err) */
-    double reserved[3];
+    int32_t no_graphs;     /* 1: launch every kernel of an SCC iteration directly instead of
+                              replaying the iteration's captured CUDA graph (debugging,
+                              profiling) */
+    int32_t reserved_i;
+    double reserved[2];
 } tb_params;
 
 typedef struct tb_report {

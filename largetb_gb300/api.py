@@ -73,7 +73,9 @@ class TbParams(C.Structure):
         ("bounds_hi", C.c_double),
         ("mode", C.c_int32),
         ("check_fp32", C.c_int32),
-        ("reserved", C.c_double * 3),
+        ("no_graphs", C.c_int32),
+        ("reserved_i", C.c_int32),
+        ("reserved", C.c_double * 2),
     ]
 
 

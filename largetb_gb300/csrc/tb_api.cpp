@@ -382,6 +382,7 @@ int ensure_work(tb_ctx *ctx)
                       w.rowgroups == rowgroups && w.nq_cap >= nq_cap && w.d && w.mom && w.T0 &&
                       w.kernel == p.kernel;
     if (same) return TB_OK;
+    ctx->gen++;  // buffers change: captured graphs are stale
     w.kernel = p.kernel;
     w.M = M;
     w.B = B;
@@ -750,6 +751,7 @@ int build_persist_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std:
 
 std::pair<cudaEvent_t, cudaEvent_t> next_events(tb_ctx *ctx)
 {
+    if (ctx->capturing) return {ctx->graph_ev[0], ctx->graph_ev[1]};
     if (ctx->ev_used == ctx->moment_events.size()) {
         cudaEvent_t a, b;
         cudaEventCreate(&a);
@@ -774,7 +776,14 @@ int density_eval(tb_ctx *ctx, bool have_shift)
     ctx->launches += 2;
 
     auto ev = next_events(ctx);
-    cudaEventRecord(ev.first, st);
+    // under stream capture an event record joins the graph only as an external node
+    auto record = [&](cudaEvent_t e) {
+        if (ctx->capturing)
+            cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+        else
+            cudaEventRecord(e, st);
+    };
+    record(ev.first);
     const int nslab = (m.n + B - 1) / B;
     for (int s = 0; s < nslab; s++) {
         const int c0 = s * B;
@@ -841,7 +850,7 @@ int density_eval(tb_ctx *ctx, bool have_shift)
             ctx->spmm_bytes += w.K * step_bytes(m, B, 4);
         }
     }
-    cudaEventRecord(ev.second, st);
+    record(ev.second);
 
     launch_moment_sums(st, w.d, m.n, M + 1, w.mom);
     ctx->launches++;
@@ -858,6 +867,71 @@ int density_eval(tb_ctx *ctx, bool have_shift)
     launch_charges(st, w.d, w.c, w.g, w.mom, M, m.n, m.natoms, w.diagP, w.q, w.state);
     ctx->launches += 3;
     TB_CUDA(cudaGetLastError());
+    return TB_OK;
+}
+
+// One SCC iteration (density evaluation + mixing update) on the stream.  The
+// iteration is captured once as a CUDA graph per configuration (ctx->gen) and
+// replayed after that: a density evaluation is ~10^3 small launches, which
+// bound the iteration for small systems.  The cooperative-launch kernels are
+// not captured; their iterations are launched directly.
+int scc_iteration(tb_ctx *ctx, bool *graphed)
+{
+    cudaStream_t st = ctx->stream;
+    DevScc &s = ctx->s;
+    DevWork &w = ctx->w;
+    *graphed = false;
+    const bool coop = w.precision == TB_PREC_FP32 && (w.kind == kKindPersistent || w.kind == kKindPipelined);
+    if (coop || ctx->p.no_graphs) {
+        TB_TRY(density_eval(ctx, true));
+        launch_scc_update(st, s, w.q, ctx->p.mix_beta, ctx->p.mix_history, ctx->p.scc_tol, w.shift, w.state);
+        ctx->launches++;
+        return TB_OK;
+    }
+    if (!ctx->scc_graph || ctx->scc_graph_gen != ctx->gen) {
+        if (ctx->scc_graph) {
+            cudaGraphExecDestroy(ctx->scc_graph);
+            ctx->scc_graph = nullptr;
+        }
+        for (cudaEvent_t &e : ctx->graph_ev)
+            if (!e) TB_CUDA(cudaEventCreate(&e));
+        const int64_t l0 = ctx->launches, s0 = ctx->spmm_launches;
+        const double b0 = ctx->spmm_bytes;
+        TB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        ctx->capturing = true;
+        int rc = density_eval(ctx, true);
+        if (rc == TB_OK) {
+            launch_scc_update(st, s, w.q, ctx->p.mix_beta, ctx->p.mix_history, ctx->p.scc_tol, w.shift, w.state);
+            ctx->launches++;
+        }
+        ctx->capturing = false;
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(st, &g);
+        if (rc == TB_OK && ec == cudaSuccess) {
+            const cudaError_t ei = cudaGraphInstantiate(&ctx->scc_graph, g, 0);
+            if (ei != cudaSuccess) {
+                ctx->scc_graph = nullptr;
+                rc = fail(ctx, TB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+            }
+        } else if (rc == TB_OK) {
+            rc = fail(ctx, TB_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(ec));
+        }
+        if (g) cudaGraphDestroy(g);
+        // nothing ran yet: the counts of the captured iteration are added per replay
+        ctx->g_launches = ctx->launches - l0;
+        ctx->g_spmm_launches = ctx->spmm_launches - s0;
+        ctx->g_spmm_bytes = ctx->spmm_bytes - b0;
+        ctx->launches = l0;
+        ctx->spmm_launches = s0;
+        ctx->spmm_bytes = b0;
+        if (rc != TB_OK) return rc;
+        ctx->scc_graph_gen = ctx->gen;
+    }
+    TB_CUDA(cudaGraphLaunch(ctx->scc_graph, st));
+    ctx->launches += ctx->g_launches;
+    ctx->spmm_launches += ctx->g_spmm_launches;
+    ctx->spmm_bytes += ctx->g_spmm_bytes;
+    *graphed = true;
     return TB_OK;
 }
 
@@ -946,6 +1020,7 @@ void begin_call(tb_ctx *ctx, cudaEvent_t *e0)
     ctx->spmm_launches = 0;
     ctx->spmm_bytes = 0.0;
     ctx->ev_used = 0;
+    ctx->extra_moment_ms = 0.0;
     cudaEventCreate(e0);
     cudaEventRecord(*e0, ctx->stream);
 }
@@ -982,7 +1057,7 @@ void fill_report(tb_ctx *ctx, cudaEvent_t e0, const DevState &hs, int iters, tb_
     rep->step_kernel = ctx->w.precision == TB_PREC_FP32 ? ctx->w.kind : 0;
     rep->precision = ctx->p.precision;
     rep->t_total_ms = tot;
-    rep->t_moments_ms = tm;
+    rep->t_moments_ms = tm + ctx->extra_moment_ms;
     rep->spmm_launches = ctx->spmm_launches;
     rep->spmm_bytes = ctx->spmm_bytes;
     rep->kernel_launches = ctx->launches;
@@ -1286,6 +1361,9 @@ int tb_ctx_destroy(tb_ctx *ctx)
         cudaEventDestroy(e.first);
         cudaEventDestroy(e.second);
     }
+    if (ctx->scc_graph) cudaGraphExecDestroy(ctx->scc_graph);
+    for (cudaEvent_t e : ctx->graph_ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return TB_OK;
@@ -1294,6 +1372,7 @@ int tb_ctx_destroy(tb_ctx *ctx)
 int tb_set_params(tb_ctx *ctx, const tb_params *p)
 {
     if (!ctx) return TB_ERR_INVALID_ARG;
+    ctx->gen++;
     TB_TRY(check_params(ctx, p));
     if (p->device != ctx->device) return fail(ctx, TB_ERR_INVALID_ARG, "device cannot change");
     const double ne = ctx->p.n_electrons;
@@ -1319,6 +1398,7 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
                        const double *vals, const int32_t *orb2atom, int32_t natoms)
 {
     if (!ctx) return TB_ERR_INVALID_ARG;
+    ctx->gen++;
     HostBsr hb;
     const int vrc = host_csr_to_bsr(n, rowptr, colidx, vals, orb2atom, natoms, hb, ctx->err);
     if (vrc) return vrc;
@@ -1354,6 +1434,7 @@ int tb_set_geometry(tb_ctx *ctx, int32_t natoms, const double *xyz, const int32_
                     const double *box, double rcut_bohr, double gamma_diag)
 {
     if (!ctx) return TB_ERR_INVALID_ARG;
+    ctx->gen++;
     if (natoms <= 0 || !xyz || !species || !box || !(rcut_bohr > 0) || !std::isfinite(gamma_diag))
         return fail(ctx, TB_ERR_INVALID_ARG, "bad geometry arguments");
     for (int d = 0; d < 3; d++) {
@@ -1421,6 +1502,7 @@ int tb_set_scc(tb_ctx *ctx, int32_t natoms, const int32_t *g_rowptr, const int32
                const double *g_vals, const double *q0)
 {
     if (!ctx) return TB_ERR_INVALID_ARG;
+    ctx->gen++;
     if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "tb_set_hamiltonian must come first");
     if (natoms != ctx->m.natoms) return fail(ctx, TB_ERR_INVALID_ARG, "natoms mismatch");
     {
@@ -1561,12 +1643,17 @@ int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, do
     std::memset(&hs, 0, sizeof(hs));
     int it = 0, rc = TB_ERR_NOT_CONVERGED;
     for (it = 1; it <= ctx->p.scc_max_iter; it++) {
-        TB_TRY(density_eval(ctx, true));
-        launch_scc_update(st, s, w.q, ctx->p.mix_beta, ctx->p.mix_history, ctx->p.scc_tol, w.shift,
-                          w.state);
-        ctx->launches++;
+        bool graphed = false;
+        TB_TRY(scc_iteration(ctx, &graphed));
         TB_CUDA(cudaGetLastError());
         TB_TRY(read_state(ctx, hs));
+        if (graphed) {  // the replay's moment phase, timed by the graph's own events
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ctx->graph_ev[0], ctx->graph_ev[1]) == cudaSuccess)
+                ctx->extra_moment_ms += ms;
+            else
+                cudaGetLastError();  // a timing gap is not an error of the solve
+        }
         if (hs.status) {
             rc = state_status(ctx, hs);
             break;

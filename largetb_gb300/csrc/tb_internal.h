@@ -162,6 +162,16 @@ struct tb_ctx {
     int tuned_kind[2][tb::kNumKinds] = {};
     int tuned_B[2][tb::kNumKinds] = {};
     // SP2 device scratch (lazily sized)
+    // SCC iteration as a CUDA graph: captured once per configuration (gen) and
+    // replayed; its moment-phase events are its own, its counts added per replay
+    uint64_t gen = 1;
+    cudaGraphExec_t scc_graph = nullptr;
+    uint64_t scc_graph_gen = 0;
+    cudaEvent_t graph_ev[2] = {nullptr, nullptr};
+    bool capturing = false;
+    int64_t g_launches = 0, g_spmm_launches = 0;
+    double g_spmm_bytes = 0.0;
+    double extra_moment_ms = 0.0;
     // FP32-vs-FP64 check of tb_density (tb_params.check_fp32): a 64-column FP64 slab
     double *chk_T0 = nullptr, *chk_T1 = nullptr, *chk_d = nullptr;
     int chk_M = 0;

@@ -299,3 +299,25 @@ def test_fp32_check_reports_recurrence_error(gpu, cfg1):
     assert np.abs(r["diagP"][:64] - ref["diagP"][:64]).max() < 1e-6
     with _ctx(gpu, m, M=200, precision=gpu.PREC_FP32) as c:
         assert c.density()["report"]["fp32_diag_err"] == 0.0
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_scc_graph_replay_equals_direct_launches(gpu, prec):
+    """The SCC iteration replayed from its captured CUDA graph gives the same
+    charges, iterations and launch counts as launching every kernel directly;
+    changing a parameter invalidates the graph."""
+    m, _ = _pair(2, 2, 2, seed=19)
+    out = {}
+    for ng in (0, 1):
+        with _ctx(gpu, m, M=160, precision=prec, no_graphs=ng) as c:
+            r = c.scc_solve()
+            c.set_params(mix_beta=0.3)
+            r2 = c.scc_solve()
+        out[ng] = (r, r2)
+    for i in (0, 1):
+        a, b = out[0][i], out[1][i]
+        assert a["iters"] == b["iters"]
+        np.testing.assert_array_equal(a["q"], b["q"])
+        assert a["report"]["kernel_launches"] == b["report"]["kernel_launches"]
+        assert a["report"]["t_moments_ms"] > 0
+    assert out[0][0]["iters"] != out[0][1]["iters"] or not np.array_equal(out[0][0]["q"], out[0][1]["q"])
