@@ -305,7 +305,12 @@ int tb_mlp_set(tb_mlp *m, const float *params, const float *norm);
  * first training set unless set before); loss_per_epoch (may be NULL). */
 int tb_mlp_train(tb_mlp *m, int32_t n, const float *feat, const float *target, int32_t epochs,
                  int32_t batch, float lr, uint64_t seed, float *loss_per_epoch);
+/* Predicted q - q0 for n atoms, on the tensor cores (tcgen05: BF16 weights
+ * and layer inputs, FP32 accumulation in tensor memory). */
 int tb_mlp_predict(tb_mlp *m, int32_t n, const float *feat, float *out);
+/* The same network on the CUDA cores with FP32 layer inputs (the training
+ * kernels' forward pass). */
+int tb_mlp_predict_fp32(tb_mlp *m, int32_t n, const float *feat, float *out);
 /* Gradient of the mean squared error w.r.t. the (BF16-rounded) parameters. */
 int tb_mlp_grad(tb_mlp *m, int32_t n, const float *feat, const float *target, float *grad,
                 float *loss);

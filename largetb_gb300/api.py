@@ -183,6 +183,7 @@ def load(build_if_missing: bool = True):
     L.tb_mlp_train.argtypes = [_vp, C.c_int32, _f32p, _f32p, C.c_int32, C.c_int32, C.c_float,
                                C.c_uint64, _vp]
     L.tb_mlp_predict.argtypes = [_vp, C.c_int32, _f32p, _f32p]
+    L.tb_mlp_predict_fp32.argtypes = [_vp, C.c_int32, _f32p, _f32p]
     L.tb_mlp_grad.argtypes = [_vp, C.c_int32, _f32p, _f32p, _f32p, _vp]
     _lib = L
     return L
@@ -529,6 +530,13 @@ class MLP:
         feat = np.ascontiguousarray(feat, np.float32)
         out = np.zeros(feat.shape[0], np.float32)
         self._chk(self._L.tb_mlp_predict(self._h, feat.shape[0], feat, out), "tb_mlp_predict")
+        return out
+
+    def predict_fp32(self, feat):
+        """The CUDA-core forward with FP32 layer inputs (tb_mlp_predict_fp32)."""
+        feat = np.ascontiguousarray(feat, np.float32)
+        out = np.zeros(feat.shape[0], np.float32)
+        self._chk(self._L.tb_mlp_predict_fp32(self._h, feat.shape[0], feat, out), "tb_mlp_predict_fp32")
         return out
 
     def grad(self, feat, target):

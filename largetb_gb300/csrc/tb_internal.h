@@ -205,6 +205,10 @@ int cheb_f32_persistent_setup(int R, size_t smem, int *ctas_per_sm);  // returns
 int launch_cheb_f32_persistent(cudaStream_t st, const DevMatrix &m, const PersistPlan &pp, int K,
                                int B, int c0, float *G0, float *G1, float2 *partial, int *flags,
                                int *err);  // returns a cudaError_t
+// ---- tb_mlp_tc.cu ----
+void launch_mlp_forward_tc(cudaStream_t st, int n, const float *X, const float *mean, const float *istd,
+                           const float *Wq, float *out, int32_t *err);
+
 // ---- tb_pipe.cu ----
 size_t cheb_f32_pipe_stage_bytes(int R, int maxU, int maxBlk, int rec_cap);
 // identity columns in the chunk-major slab layout [B/64][n][64] of the pipelined kernel

@@ -270,6 +270,7 @@ struct tb_mlp {
     cudaStream_t stream = nullptr;
     float *W = nullptr, *Wq = nullptr, *m1 = nullptr, *m2 = nullptr, *g = nullptr, *loss = nullptr;
     float *mean = nullptr, *istd = nullptr;
+    int32_t *err = nullptr;  // bounded-wait flag of the tensor-core forward
     bool have_norm = false;
     int64_t step = 0;
 };
@@ -281,7 +282,8 @@ int mlp_alloc(tb_mlp *m)
     if (cudaMalloc(&m->W, sizeof(float) * kNP) || cudaMalloc(&m->Wq, sizeof(float) * kNP) ||
         cudaMalloc(&m->m1, sizeof(float) * kNP) || cudaMalloc(&m->m2, sizeof(float) * kNP) ||
         cudaMalloc(&m->g, sizeof(float) * kNP) || cudaMalloc(&m->loss, sizeof(float)) ||
-        cudaMalloc(&m->mean, sizeof(float) * kF) || cudaMalloc(&m->istd, sizeof(float) * kF))
+        cudaMalloc(&m->mean, sizeof(float) * kF) || cudaMalloc(&m->istd, sizeof(float) * kF) ||
+        cudaMalloc(&m->err, sizeof(int32_t)) || cudaMemset(m->err, 0, sizeof(int32_t)))
         return TB_ERR_OUT_OF_MEMORY;
     return TB_OK;
 }
@@ -389,6 +391,7 @@ int tb_mlp_destroy(tb_mlp *m)
     cudaFree(m->loss);
     cudaFree(m->mean);
     cudaFree(m->istd);
+    cudaFree(m->err);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
     return TB_OK;
@@ -444,6 +447,29 @@ int tb_mlp_grad(tb_mlp *m, int32_t n, const float *feat, const float *target, fl
 }
 
 int tb_mlp_predict(tb_mlp *m, int32_t n, const float *feat, float *out)
+{
+    if (!m || n <= 0 || !feat || !out) return TB_ERR_INVALID_ARG;
+    cudaSetDevice(m->device);
+    float *dX = nullptr, *dY = nullptr;
+    int rc = upload_set(m->stream, n, feat, nullptr, &dX, nullptr);
+    if (rc == TB_OK && cudaMalloc(&dY, sizeof(float) * n)) rc = TB_ERR_OUT_OF_MEMORY;
+    if (rc == TB_OK) {
+        launch_mlp_forward_tc(m->stream, n, dX, m->mean, m->istd, m->Wq, dY, m->err);
+        int32_t e = 0;
+        cudaMemcpyAsync(out, dY, sizeof(float) * n, cudaMemcpyDeviceToHost, m->stream);
+        cudaMemcpyAsync(&e, m->err, sizeof(int32_t), cudaMemcpyDeviceToHost, m->stream);
+        if (cudaStreamSynchronize(m->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = TB_ERR_CUDA;
+        if (rc == TB_OK && e) {
+            cudaMemsetAsync(m->err, 0, sizeof(int32_t), m->stream);
+            rc = TB_ERR_CUDA;
+        }
+    }
+    cudaFree(dX);
+    cudaFree(dY);
+    return rc;
+}
+
+int tb_mlp_predict_fp32(tb_mlp *m, int32_t n, const float *feat, float *out)
 {
     if (!m || n <= 0 || !feat || !out) return TB_ERR_INVALID_ARG;
     cudaSetDevice(m->device);

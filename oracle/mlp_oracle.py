@@ -77,6 +77,19 @@ def forward(params, norm, feat):
     return h2 @ w3 + b3, (x, z1, h1, z2, h2, W2, w3)
 
 
+def forward_bf16_inputs(params, norm, feat):
+    """forward() with each layer's input rounded to BF16 as well -- the
+    numerics of the tensor-core inference kernel (the normalisation in FP32,
+    as on the device)."""
+    q = bf16(params)
+    W1, b1, W2, b2, w3, b3 = unpack(q)
+    mean, istd = np.asarray(norm[:NF], np.float32), np.asarray(norm[NF:], np.float32)
+    x = bf16((np.asarray(feat, np.float32) - mean) * istd)
+    h1 = silu(x @ W1.T + b1)
+    z2 = bf16(h1) @ W2.T + b2
+    return silu(z2) @ w3 + b3
+
+
 def grad(params, norm, feat, target):
     y, (x, z1, h1, z2, h2, W2, w3) = forward(params, norm, feat)
     n = y.shape[0]

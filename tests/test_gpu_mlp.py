@@ -34,7 +34,7 @@ def test_gradients_match_oracle(gpu):
     assert abs(loss - lr) < 1e-5 * max(1.0, lr)
     scale = np.abs(gr).max()
     np.testing.assert_allclose(g, gr, atol=2e-5 * scale, rtol=0)
-    y = mlp.predict(X)
+    y = mlp.predict_fp32(X)  # the training kernels' forward (FP32 layer inputs)
     yr, _ = MO.forward(p, nrm, X.astype(np.float64))
     np.testing.assert_allclose(y, yr, atol=2e-5 * max(1.0, np.abs(yr).max()), rtol=0)
 
@@ -58,3 +58,26 @@ def test_learned_start_cuts_scc_iterations(gpu):
     err0 = np.abs(held.q0 - zero["q"]).max()
     errw = np.abs(q_init - zero["q"]).max()
     assert errw < 0.5 * err0
+
+
+def test_tensor_core_forward_matches_oracle(gpu):
+    """tb_mlp_predict runs the dense layers on tcgen05 (BF16 layer inputs,
+    FP32 accumulation in tensor memory): against the oracle with the same
+    BF16 rounding, on a ragged atom count (648 = 5 x 128 + 8); the CUDA-core
+    FP32 forward against the FP64 oracle; the shipped weights through both."""
+    from largetb_gb300 import learned
+    m = gpu.model_cristobalite(3, 3, 3, sigma_ang=0.1, seed=21)
+    X = gpu.mlp_features(m.xyz, m.species, learned.cell_box((3, 3, 3)))
+    mlp = gpu.MLP(seed=5)
+    nrm = np.concatenate([X.mean(0), 1.0 / (X.std(0) + 1e-3)]).astype(np.float32)
+    mlp.set(norm=nrm)
+    p, _ = mlp.get()
+    y_tc, y32 = mlp.predict(X), mlp.predict_fp32(X)
+    yb = MO.forward_bf16_inputs(p, nrm, X)
+    yr, _ = MO.forward(p, nrm, X.astype(np.float64))
+    scale = max(1.0, np.abs(yr).max())
+    np.testing.assert_allclose(y_tc, yb, atol=2e-3 * scale, rtol=0)
+    np.testing.assert_allclose(y32, yr, atol=2e-5 * scale, rtol=0)
+    trained = learned.load()
+    a, b = trained.predict(X), trained.predict_fp32(X)
+    assert np.abs(a - b).max() < 0.02 and np.abs(a).max() > 0.1
