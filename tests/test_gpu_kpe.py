@@ -321,3 +321,23 @@ def test_scc_graph_replay_equals_direct_launches(gpu, prec):
         assert a["report"]["kernel_launches"] == b["report"]["kernel_launches"]
         assert a["report"]["t_moments_ms"] > 0
     assert out[0][0]["iters"] != out[0][1]["iters"] or not np.array_equal(out[0][0]["q"], out[0][1]["q"])
+
+
+def test_large_cell_properties(gpu):
+    """8x8x8 cristobalite (12288 atoms, 49152 orbitals), M = 200, FP32 form
+    with the autotuned kernel: size-independent properties -- the electron
+    count, 0 <= diagP <= 1, the in-call FP64 check of 64 columns within the
+    1e-6 e bar, and the two pipelined launch modes agreeing to round-off."""
+    m = gpu.model_cristobalite(8, 8, 8, sigma_ang=0.08, seed=8008)
+    with _ctx(gpu, m, M=200, precision=gpu.PREC_FP32, check_fp32=1) as c:
+        r = c.density()
+    rep = r["report"]
+    assert abs(r["q"].sum() - m.n_electrons) < 1e-5
+    assert r["diagP"].min() > -1e-6 and r["diagP"].max() < 1 + 1e-6
+    assert rep["fp32_diag_err"] < 1e-6
+    out = {}
+    for kern in (3, 4):
+        with _ctx(gpu, m, M=200, precision=gpu.PREC_FP32, fp32_kernel=kern, column_block=1024) as c:
+            out[kern] = c.density()
+    assert np.array_equal(out[3]["moments"], out[4]["moments"])
+    assert np.abs(out[4]["q"] - r["q"]).max() < 1e-9
