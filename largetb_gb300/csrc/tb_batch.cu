@@ -885,7 +885,8 @@ int batch_build(tb_batch *b)
     // the staged step needs all of its shared memory opted in
     const size_t smem = bt_smem(maxU, maxBlk);
     if (smem > 227 * 1024) return bfail(b, TB_ERR_UNSUPPORTED, "row-group halo too large for shared memory");
-    cudaError_t e = cudaFuncSetAttribute(k_bt_cheb_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_bt_cheb_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         smem_optin_max((const void *)k_bt_cheb_f32));
     if (e != cudaSuccess) return bfail(b, TB_ERR_CUDA, cudaGetErrorString(e));
     e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) return bfail(b, TB_ERR_CUDA, cudaGetErrorString(e));

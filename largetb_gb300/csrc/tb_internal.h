@@ -181,6 +181,22 @@ struct tb_ctx {
 
 namespace tb {
 
+// The most dynamic shared memory kernel `func` can opt in to on the current
+// device: the per-block opt-in limit less the kernel's static shared memory.
+// Kernels opt in to all of it: the attribute is per process, so a smaller
+// value set for one context's plan must not cap another context's launches
+// (the launch's own size still decides occupancy).
+inline int smem_optin_max(const void *func)
+{
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (v <= 0) v = 227 * 1024;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, func) == cudaSuccess) v -= (int)fa.sharedSizeBytes;
+    return v;
+}
+
 // ---- launchers implemented in tb_kpe.cu ----------------------------------
 void launch_coulomb_shift(cudaStream_t st, const DevScc &s, const double *q, double *V,
                           double *shift);

@@ -585,8 +585,9 @@ __global__ void __launch_bounds__(32 * kV2Warps)
 
 int cheb_f32_staged_configure(size_t smem)
 {
-    return (int)cudaFuncSetAttribute(k_cheb_f32_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem);
+    const int lim = smem_optin_max((const void *)k_cheb_f32_staged);
+    if ((int)smem > lim) return (int)cudaErrorInvalidValue;
+    return (int)cudaFuncSetAttribute(k_cheb_f32_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
 }
 
 size_t cheb_f32_staged_smem(int R, int maxU, int maxBlk)
@@ -853,8 +854,9 @@ static int persistent_rpw(int R) { return (R + kPWarps - 1) / kPWarps; }
 template <int kRPW>
 static int persistent_setup_t(size_t smem, int *ctas_per_sm)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_cheb_f32_persistent<kRPW>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int lim = smem_optin_max((const void *)k_cheb_f32_persistent<kRPW>);
+    if ((int)smem > lim) return (int)cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_cheb_f32_persistent<kRPW>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (e != cudaSuccess) return (int)e;
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_cheb_f32_persistent<kRPW>,
                                                               32 * kPWarps, smem);

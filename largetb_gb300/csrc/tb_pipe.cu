@@ -489,7 +489,9 @@ int cheb_f32_pipe_max_rows() { return kPipeCW * 3; }
 
 int cheb_f32_pipe_configure(size_t smem, int *ctas_per_sm)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_cheb_f32_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int lim = smem_optin_max((const void *)k_cheb_f32_pipe);
+    if ((int)smem > lim) return (int)cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_cheb_f32_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (e != cudaSuccess) return (int)e;
     *ctas_per_sm = 0;
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_cheb_f32_pipe, kPipeThreads, smem);

@@ -452,7 +452,8 @@ int sp2_run(tb_ctx *ctx, double *diagP_h, double *q_h, double *e_band, tb_report
     int nsm = 152;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
     int grid = std::min(nb, nsm * (acc_smem ? std::max(1, (int)(227 * 1024 / (smem + 1024))) : 4));
-    if ((e = cudaFuncSetAttribute(k_sp2_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) {
+    if ((e = cudaFuncSetAttribute(k_sp2_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem_optin_max((const void *)k_sp2_step<T>)))) {
         cuda_fail(e, "cudaFuncSetAttribute(k_sp2_step)");
         return rc;
     }

@@ -341,3 +341,18 @@ def test_large_cell_properties(gpu):
             out[kern] = c.density()
     assert np.array_equal(out[3]["moments"], out[4]["moments"])
     assert np.abs(out[4]["q"] - r["q"]).max() < 1e-9
+
+
+def test_contexts_with_different_plans_coexist(gpu):
+    """Two live contexts whose pipelined plans need different shared memory:
+    the later (smaller) plan must not cap the earlier context's launches."""
+    big = gpu.model_cristobalite(2, 2, 3, sigma_ang=0.05, seed=41)    # R = 24 groups
+    small = gpu.model_cristobalite(1, 1, 1, sigma_ang=0.05, seed=42)  # a different R
+    a = _ctx(gpu, big, M=80, precision=gpu.PREC_FP32, fp32_kernel=4, column_block=256)
+    ra = a.density()
+    b = _ctx(gpu, small, M=80, precision=gpu.PREC_FP32, fp32_kernel=4, column_block=128)
+    b.density()
+    ra2 = a.density()
+    np.testing.assert_array_equal(ra["q"], ra2["q"])
+    a.close()
+    b.close()
