@@ -700,6 +700,10 @@ struct tb_batch {
     int units_cap = 0;
     DevState *st = nullptr;
     std::vector<int32_t> h_ao, h_B, h_g0, h_grpI0;
+    // the SCC iteration as a CUDA graph, captured per active set (its grid
+    // sizes and unit list change only when a structure converges)
+    cudaGraphExec_t graph = nullptr;
+    std::vector<int32_t> graph_act;
 };
 
 namespace {
@@ -742,6 +746,10 @@ void bfree(tb_batch *b)
 int batch_build(tb_batch *b)
 {
     bfree(b);
+    if (b->graph) {  // captured against the buffers being replaced
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
     const int S = b->S;
     const int M = b->p.M;
     b->M = M;
@@ -940,6 +948,7 @@ int tb_batch_destroy(tb_batch *b)
     cudaSetDevice(b->p.device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     bfree(b);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->units) cudaFree(b->units);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -1016,6 +1025,10 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
             act_cols += 4 * (b->h_ao[s + 1] - b->h_ao[s]);
         }
         if ((int)units.size() > b->units_cap) {
+            if (b->graph) {  // holds the old unit-list pointer
+                cudaGraphExecDestroy(b->graph);
+                b->graph = nullptr;
+            }
             if (b->units) cudaFree(b->units);
             b->units_cap = (int)units.size();
             if (cudaMalloc(&b->units, sizeof(Unit) * b->units_cap) != cudaSuccess) {
@@ -1025,31 +1038,87 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
                 break;
             }
         }
-        cudaMemcpyAsync(b->units, units.data(), sizeof(Unit) * units.size(), cudaMemcpyHostToDevice, st);
         const int nu = (int)units.size();
-        k_bt_gershgorin<<<S, 1024, 0, st>>>(b->s_ao, b->h0diag, b->radius, b->shift, b->active, b->p.kT, M,
-                                            b->nq_cap, b->st);
-        k_bt_build_x<<<(unsigned)((b->nnzb * 16 + 255) / 256), 256, 0, st>>>(
-            b->nnzb, b->blkrow, b->colidx, b->s_of_atom, b->active, b->h0, b->shift, b->st, b->x32, b->xdiag32);
-        cudaEventRecord(m0, st);
-        k_bt_identity<<<nu, 256, 0, st>>>(b->units, nu, b->s_ao, b->s_B, b->s_toff, b->grp_I0, b->T0);
-        launches += 3;
-        for (int k = 0; k < K; k++) {
-            const bool odd = (k + 1) & 1;
-            const float *Tin = odd ? b->T0 : b->T1;
-            float *Tout = odd ? b->T1 : b->T0;
-            k_bt_cheb_f32<<<nu, 32 * kBtWarps, smem, st>>>(b->units, b->s_ao, b->s_B, b->s_toff, b->s_poff,
-                                                            b->s_g0, b->grp_I0, b->rowptr, b->lcol, b->lself,
-                                                            b->grp_ptr, b->grp_rows, b->x32, Tin, Tout, k == 0,
-                                                            reinterpret_cast<float2 *>(b->partial), b->maxU,
-                                                            b->maxBlk);
-            k_bt_finalize<<<(n + 255) / 256, 256, 0, st>>>(n, k, M, b->s_of_atom, b->active, b->s_ao, b->s_B,
-                                                           b->s_poff, b->s_g0,
-                                                           reinterpret_cast<const float2 *>(b->partial),
-                                                           b->xdiag32, b->d);
-            launches += 2;
+        // The iteration's kernels: captured as a CUDA graph once per active
+        // set (grid sizes and the unit list change only when a structure
+        // converges) and replayed after that, or issued directly (no_graphs).
+        const bool use_graph = !b->p.no_graphs;
+        const bool fresh = !b->graph || b->graph_act != act;
+        if (fresh || !use_graph)
+            cudaMemcpyAsync(b->units, units.data(), sizeof(Unit) * units.size(), cudaMemcpyHostToDevice, st);
+        const bool capture = use_graph && fresh;
+        auto record = [&](cudaEvent_t e) {
+            if (capture)
+                cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+            else
+                cudaEventRecord(e, st);
+        };
+        auto issue = [&]() {
+            k_bt_gershgorin<<<S, 1024, 0, st>>>(b->s_ao, b->h0diag, b->radius, b->shift, b->active, b->p.kT, M,
+                                                b->nq_cap, b->st);
+            k_bt_build_x<<<(unsigned)((b->nnzb * 16 + 255) / 256), 256, 0, st>>>(
+                b->nnzb, b->blkrow, b->colidx, b->s_of_atom, b->active, b->h0, b->shift, b->st, b->x32, b->xdiag32);
+            record(m0);
+            k_bt_identity<<<nu, 256, 0, st>>>(b->units, nu, b->s_ao, b->s_B, b->s_toff, b->grp_I0, b->T0);
+            for (int k = 0; k < K; k++) {
+                const bool odd = (k + 1) & 1;
+                const float *Tin = odd ? b->T0 : b->T1;
+                float *Tout = odd ? b->T1 : b->T0;
+                k_bt_cheb_f32<<<nu, 32 * kBtWarps, smem, st>>>(b->units, b->s_ao, b->s_B, b->s_toff, b->s_poff,
+                                                                b->s_g0, b->grp_I0, b->rowptr, b->lcol, b->lself,
+                                                                b->grp_ptr, b->grp_rows, b->x32, Tin, Tout, k == 0,
+                                                                reinterpret_cast<float2 *>(b->partial), b->maxU,
+                                                                b->maxBlk);
+                k_bt_finalize<<<(n + 255) / 256, 256, 0, st>>>(n, k, M, b->s_of_atom, b->active, b->s_ao, b->s_B,
+                                                               b->s_poff, b->s_g0,
+                                                               reinterpret_cast<const float2 *>(b->partial),
+                                                               b->xdiag32, b->d);
+            }
+            record(m1);
+            k_bt_moment_sums<<<dim3(M + 1, S), 256, 0, st>>>(b->d, n, M, b->s_ao, b->active, b->mom);
+            if (b->p.kT > 0)
+                k_bt_dos_nodes<<<dim3(64, S), 256, 0, st>>>(b->g, b->mom, M, b->st, b->active, b->nq_cap, b->rho);
+            for (int r = 0; r < kBisectRounds; r++)
+                k_bt_bisect<<<dim3(kBisectCand, S), 256, 0, st>>>(b->rho, b->nq_cap, b->g, b->mom, M, b->ne,
+                                                                  b->p.mu_tol, r, kBisectRounds - 1, b->active,
+                                                                  b->cand, b->st);
+            k_bt_coeffs<<<dim3(M, S), 256, 0, st>>>(M, b->st, b->active, b->c);
+            k_bt_charges<<<(na + 255) / 256, 256, 0, st>>>(b->d, b->c, b->g, M, n, na, b->s_of_atom, b->active,
+                                                           b->diagP, b->q);
+            k_bt_eband<<<S, 256, 0, st>>>(b->c, b->g, b->mom, M, b->active, b->st);
+            k_bt_scc_update<<<S, 1024, 0, st>>>(b->s_ao, b->q, b->qin, b->q0d, b->hq, b->hr, na, b->meta,
+                                                b->p.mix_beta, b->p.mix_history, b->p.scc_tol, b->g_rp, b->g_ci,
+                                                b->g_v, b->shift, b->active, b->st);
+        };
+        if (capture) {
+            if (b->graph) {
+                cudaGraphExecDestroy(b->graph);
+                b->graph = nullptr;
+            }
+            cudaError_t ec = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+            if (ec == cudaSuccess) {
+                issue();
+                cudaGraph_t gr = nullptr;
+                ec = cudaStreamEndCapture(st, &gr);
+                if (ec == cudaSuccess) ec = cudaGraphInstantiate(&b->graph, gr, 0);
+                if (gr) cudaGraphDestroy(gr);
+            }
+            if (ec != cudaSuccess) {
+                b->graph = nullptr;
+                rc = bfail(b, TB_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ec));
+                break;
+            }
+            b->graph_act = act;
         }
-        cudaEventRecord(m1, st);
+        if (use_graph) {
+            if (cudaGraphLaunch(b->graph, st) != cudaSuccess) {
+                rc = bfail(b, TB_ERR_CUDA, "cudaGraphLaunch (batch)");
+                break;
+            }
+        } else {
+            issue();
+        }
+        launches += 3 + 2 * (int64_t)K + 6 + kBisectRounds - (b->p.kT > 0 ? 0 : 1);
         spmm += K;
         // algorithmic bytes of a batched step: the sum over active structures
         // of nnzb_s (16 s + 4) + (nb_s + 1) 4 + 3 n_s B_s s, s = 4
@@ -1059,20 +1128,6 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
                 const double nnzb_s = (double)b->hb[s].bcol.size();
                 spmm_bytes += K * (nnzb_s * 68.0 + (nb_s + 1) * 4.0 + 3.0 * 4 * nb_s * (double)b->h_B[s] * 4.0);
             }
-        k_bt_moment_sums<<<dim3(M + 1, S), 256, 0, st>>>(b->d, n, M, b->s_ao, b->active, b->mom);
-        if (b->p.kT > 0)
-            k_bt_dos_nodes<<<dim3(64, S), 256, 0, st>>>(b->g, b->mom, M, b->st, b->active, b->nq_cap, b->rho);
-        for (int r = 0; r < kBisectRounds; r++)
-            k_bt_bisect<<<dim3(kBisectCand, S), 256, 0, st>>>(b->rho, b->nq_cap, b->g, b->mom, M, b->ne, b->p.mu_tol,
-                                                              r, kBisectRounds - 1, b->active, b->cand, b->st);
-        k_bt_coeffs<<<dim3(M, S), 256, 0, st>>>(M, b->st, b->active, b->c);
-        k_bt_charges<<<(na + 255) / 256, 256, 0, st>>>(b->d, b->c, b->g, M, n, na, b->s_of_atom, b->active,
-                                                       b->diagP, b->q);
-        k_bt_eband<<<S, 256, 0, st>>>(b->c, b->g, b->mom, M, b->active, b->st);
-        k_bt_scc_update<<<S, 1024, 0, st>>>(b->s_ao, b->q, b->qin, b->q0d, b->hq, b->hr, na, b->meta,
-                                            b->p.mix_beta, b->p.mix_history, b->p.scc_tol, b->g_rp, b->g_ci,
-                                            b->g_v, b->shift, b->active, b->st);
-        launches += 6 + kBisectRounds;
         cudaMemcpyAsync(act.data(), b->active, sizeof(int32_t) * S, cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(hs.data(), b->st, sizeof(DevState) * S, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);

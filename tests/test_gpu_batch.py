@@ -54,3 +54,21 @@ def test_batch_unset_structure_is_reported(gpu):
     rc = L.tb_batch_scc_solve(h, None, None, None, None, None, C.byref(rep))
     assert rc == gpu.api.TB_ERR_NOT_READY
     L.tb_batch_destroy(h)
+
+
+def test_batch_graph_replay_equals_direct_launches(gpu):
+    """The batched SCC iteration replayed from graphs captured per active set
+    equals launching every kernel directly; a second solve reuses the batch."""
+    models = [gpu.model_cristobalite(*c, sigma_ang=s, seed=sd) for c, s, sd in CASES]
+    out = {}
+    for ng in (0, 1):
+        with gpu.Batch(models, M=120, no_graphs=ng) as b:
+            r1 = b.scc_solve()
+            r2 = b.scc_solve()
+        out[ng] = (r1, r2)
+    for i in (0, 1):
+        a, c = out[0][i], out[1][i]
+        np.testing.assert_array_equal(np.asarray(a["iters"]), np.asarray(c["iters"]))
+        for qa, qc in zip(a["q"], c["q"]):
+            np.testing.assert_array_equal(qa, qc)
+        assert a["report"]["kernel_launches"] == c["report"]["kernel_launches"]
