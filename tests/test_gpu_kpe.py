@@ -356,3 +356,40 @@ def test_contexts_with_different_plans_coexist(gpu):
     np.testing.assert_array_equal(ra["q"], ra2["q"])
     a.close()
     b.close()
+
+
+def test_edge_sizes(gpu):
+    """Empty and mismatched inputs are refused with a status; a single
+    isolated atom (one 4x4 diagonal block, a ragged 4-column slab) gives the
+    occupations of its own levels; the smallest and largest expansion orders
+    run (M = 2, M = 6000) and M = 6001 is refused."""
+    import largetb_gb300 as T
+    with T.Context() as c:
+        e0 = np.zeros(0, np.int32)
+        with pytest.raises(T.TbError) as e:
+            c.set_hamiltonian(np.zeros(1, np.int32), e0, np.zeros(0), e0, 0)
+        assert e.value.status == T.api.TB_ERR_INVALID_ARG
+        rp = np.arange(0, 17, 4, dtype=np.int32)
+        ci = np.tile(np.arange(4, dtype=np.int32), 4)
+        with pytest.raises(T.TbError) as e:  # 4 orbitals declared as 2 atoms
+            c.set_hamiltonian(rp, ci, np.eye(4).ravel(), np.array([0, 0, 1, 1], np.int32), 2)
+        assert e.value.status == T.api.TB_ERR_STRUCTURE
+    # one isolated atom: levels -0.5 (s) and 0.2 (p x3), 2 electrons fill the s level
+    h = np.diag([-0.5, 0.2, 0.2, 0.2]).ravel()
+    for prec in (0, 1):
+        with T.Context(M=400, kT=0.005, n_electrons=2.0, precision=prec, spectral_pad=0.05) as c:
+            c.set_hamiltonian(rp, ci, h, np.zeros(4, np.int32), 1)
+            r = c.density()
+        np.testing.assert_allclose(r["diagP"], [1, 0, 0, 0], atol=1e-4)
+        assert abs(r["q"][0] - 2.0) < 1e-6
+    m, o = _pair(1, 1, 1, seed=3)
+    for M in (2, 6000):
+        with _ctx(gpu, m, M=M, precision=1, kT=0.05) as c:
+            r = c.density()
+        assert abs(r["q"].sum() - m.n_electrons) < 1e-5
+        if M == 6000:
+            ref = O.density(o, O.kpe_params(M=M, kT=0.05, n_elec=o.n_elec))
+            assert np.abs(r["q"] - ref["q"]).max() < 1e-6
+    p = T.params(M=6001)
+    h_ = T.api._vp()
+    assert T.load().tb_ctx_create(T.api.C.byref(p), T.api.C.byref(h_)) == T.api.TB_ERR_INVALID_ARG
