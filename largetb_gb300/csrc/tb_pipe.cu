@@ -21,8 +21,8 @@
 // Two launch modes share the kernel:
 //  - one launch per step (steps = 1);
 //  - one cooperative launch per slab running all K steps.  A tile publishes
-//    its step count in flags[tile] (release, after a CTA barrier over its
-//    stores); before the producer copies tile (chunk, g) of step k >= 1 it
+//    its step count in flags[tile] (release, after an mbarrier that every
+//    consumer warp arrives on after its stores); before the producer copies tile (chunk, g) of step k >= 1 it
 //    waits (acquire) until every group g' whose rows g references, g itself
 //    included, has published step k in the same chunk.  That covers both the
 //    T_k rows it reads and the T_{k-1} rows it overwrites: the block pattern is
@@ -37,15 +37,19 @@
 // b' = s - a), its exact rounding error collected in lo.  GB300 issues FP64 at
 // about 2 operations per clock per SM, so per-row FP64 accumulation would cost
 // as much as the rest of the step; the pairs keep ~44 significant bits with
-// FP32 arithmetic only.  The consumer warps' pairs are summed in a fixed order
-// through a shared array (two named barriers per tile), giving
-// partial[k][g][col][2] as float2 (hi, lo); k_f32_finalize_pairs converts to
+// FP32 arithmetic only.  The recurrence itself and the per-row products use
+// packed FP32 pair instructions (fma.f32x2 / add.f32x2: two columns per
+// instruction, each rounded as the scalar operation).  Each consumer warp
+// hands its pairs over in a shared array and arrives on an mbarrier; four
+// consumer warps, in rotation from tile to tile, wait for all twelve and sum
+// them in warp order, giving partial[k][g][col][2] as float2 (hi, lo), while
+// the other warps go on with the next tile.  k_f32_finalize_pairs converts to
 // FP64.
 //
 // Every wait is bounded: after kPipeSpin unsuccessful polls the thread raises
-// a block-wide abort flag and the device error flag; all consumer warps still
-// run the same tile sequence (so the named barriers stay matched) but skip the
-// work, other CTAs waiting on this one's flags time out the same way, and the
+// a block-wide abort flag and the device error flag; every later wait in the
+// CTA then returns at once, the warps run out their tile sequence skipping
+// the work, other CTAs waiting on this one's flags time out the same way, and the
 // producer, before it returns, waits (again bounded) for the copies it has
 // issued.
 #include <cuda_runtime.h>
@@ -62,6 +66,8 @@ constexpr int kPipeCols = 64;
 constexpr int kPipeCW = 12;  // consumer warps; then one producer and one publisher warp
 constexpr int kPipeThreads = 32 * (kPipeCW + 2);
 constexpr int kPubSlots = 4;  // tiles the publisher may lag behind the consumers
+constexpr int kRedWarps = 4;  // consumer warps that reduce one tile's column sums, in rotation
+static_assert(kPipeCW % kRedWarps == 0 && kRedWarps * 32 == 2 * kPipeCols, "reducer split");
 constexpr uint32_t kPipeSpin = 1u << 22;  // mbarrier polls
 constexpr uint32_t kFlagSpin = 1u << 22;  // neighbour-flag polls (~128 ns apart)
 
@@ -154,9 +160,16 @@ __device__ __forceinline__ void pair_add(float &s, float &c, float x)
     c += e;
 }
 
-__device__ __forceinline__ void consumer_sync()
+// pair_add on both components of packed FP32 pairs; fma(-1, a, b) is b - a
+// with the same single rounding
+__device__ __forceinline__ void pair_add2(float2 &s, float2 &c, float2 x)
 {
-    asm volatile("bar.sync 1, %0;\n" ::"r"(32 * kPipeCW) : "memory");
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 t = __fadd2_rn(s, x);
+    const float2 bp = __ffma2_rn(m1, s, t);
+    const float2 e = __fadd2_rn(__ffma2_rn(m1, __ffma2_rn(m1, bp, t), s), __ffma2_rn(m1, bp, x));
+    s = t;
+    c = __fadd2_rn(c, e);
 }
 
 // Poll until the phase of the given parity completes; false on abort or
@@ -223,7 +236,9 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
     uint64_t *empty = full + a.stages;
     uint64_t *pub = empty + a.stages;       // consumers -> publisher: tile done
     uint64_t *pubfree = pub + kPubSlots;    // publisher -> consumers: slot free again
-    volatile int *s_abort = reinterpret_cast<volatile int *>(pubfree + kPubSlots);
+    uint64_t *redfull = pubfree + kPubSlots;  // consumer warps -> reducers: red[] holds the tile's sums
+    uint64_t *redfree = redfull + 1;          // reducers -> consumer warps: red[] read
+    volatile int *s_abort = reinterpret_cast<volatile int *>(redfree + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         for (int s = 0; s < a.stages; s++) {
@@ -234,6 +249,8 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
             mbar_init(&pub[s], 1);
             mbar_init(&pubfree[s], 1);
         }
+        mbar_init(redfull, kPipeCW);
+        mbar_init(redfree, kRedWarps);
         *s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
@@ -349,8 +366,9 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         const int chunk = t / a.G, g = t - chunk * a.G;
         const int I0 = g * a.R, nr = min(a.nb, I0 + a.R) - I0;
         float *out = ((k & 1) ? a.T0 : a.T1) + (int64_t)chunk * chunk_floats + (int64_t)I0 * 4 * kPipeCols + c;
-        // pairs (hi, lo): [0] <T_k,T_k> col c, [1] <T_k,T_{k+1}> col c, [2], [3] the same for col c+1
-        float hs[4] = {0.f, 0.f, 0.f, 0.f}, ls[4] = {0.f, 0.f, 0.f, 0.f};
+        // pairs (hi, lo), packed over columns (c, c+1): <T_k,T_k> in (eh, el),
+        // <T_k,T_{k+1}> in (oh, ol)
+        float2 eh = make_float2(0.f, 0.f), el = eh, oh = eh, ol = eh;
         if (wait_phase(&full[s], (uint32_t)(i / a.stages) & 1u, s_abort, a.err)) {
             const float *stg = reinterpret_cast<const float *>(smem + (size_t)s * a.stage_bytes);
             const float *sT = stg + oT, *sP = stg + oP, *sX = stg + oX;
@@ -358,9 +376,12 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
             const int32_t *sLc = sRp + nr + 1;
             const int32_t *sLs = sLc + sRp[nr];
             for (int r = warp; r < nr; r += kPipeCW) {
-                float acc[4][2];
+                // acc[q] = row q of the block row, columns (c, c+1): packed
+                // FP32 pairs, one fma.f32x2 per (q, m), each component
+                // rounded exactly as fmaf
+                float2 acc[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++) acc[q][0] = acc[q][1] = 0.f;
+                for (int q = 0; q < 4; q++) acc[q] = make_float2(0.f, 0.f);
                 const int ta = sRp[r], te = sRp[r + 1];
                 for (int tt = ta; tt < te; tt++) {
                     const float *tv = sT + sLc[tt] * 4 * kPipeCols + c;
@@ -371,49 +392,50 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
 #pragma unroll
                     for (int q = 0; q < 4; q++) {
                         const float4 xr = xb[q];
-                        const float xm[4] = {xr.x, xr.y, xr.z, xr.w};
-#pragma unroll
-                        for (int m = 0; m < 4; m++) {
-                            acc[q][0] = fmaf(xm[m], v[m].x, acc[q][0]);
-                            acc[q][1] = fmaf(xm[m], v[m].y, acc[q][1]);
-                        }
+                        acc[q] = __ffma2_rn(make_float2(xr.x, xr.x), v[0], acc[q]);
+                        acc[q] = __ffma2_rn(make_float2(xr.y, xr.y), v[1], acc[q]);
+                        acc[q] = __ffma2_rn(make_float2(xr.z, xr.z), v[2], acc[q]);
+                        acc[q] = __ffma2_rn(make_float2(xr.w, xr.w), v[3], acc[q]);
                     }
                 }
                 const float *own = sT + sLs[r] * 4 * kPipeCols + c;
-                float ee0 = 0.f, ee1 = 0.f, eo0 = 0.f, eo1 = 0.f;
+                float2 ee = make_float2(0.f, 0.f), eo = ee;
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     const float2 ov = *reinterpret_cast<const float2 *>(own + q * kPipeCols);
-                    float2 o;
-                    if (k == 0) {
-                        o = make_float2(acc[q][0], acc[q][1]);
-                    } else {
+                    float2 o = acc[q];
+                    if (k > 0) {  // 2 acc - p: exact doubling, then fma(-1, p, 2 acc) rounds once
                         const float2 p = *reinterpret_cast<const float2 *>(sP + (r * 4 + q) * kPipeCols + c);
-                        o.x = 2.f * acc[q][0] - p.x;
-                        o.y = 2.f * acc[q][1] - p.y;
+                        o = __ffma2_rn(make_float2(-1.f, -1.f), p, __fadd2_rn(acc[q], acc[q]));
                     }
                     *reinterpret_cast<float2 *>(out + (r * 4 + q) * kPipeCols) = o;
-                    ee0 = fmaf(ov.x, ov.x, ee0);
-                    ee1 = fmaf(ov.y, ov.y, ee1);
-                    eo0 = fmaf(ov.x, o.x, eo0);
-                    eo1 = fmaf(ov.y, o.y, eo1);
+                    ee = __ffma2_rn(ov, ov, ee);
+                    eo = __ffma2_rn(ov, o, eo);
                 }
-                pair_add(hs[0], ls[0], ee0);
-                pair_add(hs[1], ls[1], eo0);
-                pair_add(hs[2], ls[2], ee1);
-                pair_add(hs[3], ls[3], eo1);
+                pair_add2(eh, el, ee);
+                pair_add2(oh, ol, eo);
             }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);  // stage s may be refilled
-        if (i > 0) consumer_sync();             // the previous tile's sums have been read
-        float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)warp * kPipeCols + c) * 4);
-        rb[0] = make_float4(hs[0], ls[0], hs[1], ls[1]);
-        rb[1] = make_float4(hs[2], ls[2], hs[3], ls[3]);
-        consumer_sync();  // also: every consumer's T_{k+1} stores of this tile precede it
-        if (!*s_abort) {
-            if (tid < 2 * kPipeCols) {
-                const int j = tid >> 1, which = tid & 1;
+        // Hand this warp's sums over in red[warp]; the buffer is free again once
+        // the previous tile's reducers have read it.  Neither phase below can
+        // complete twice before it is polled: the next phase of redfull needs
+        // this tile's redfree, and the next phase of redfree needs this warp's
+        // arrival on redfull.
+        if (i == 0 || wait_phase(redfree, (uint32_t)(i - 1) & 1u, s_abort, a.err)) {
+            float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)warp * kPipeCols + c) * 4);
+            rb[0] = make_float4(eh.x, el.x, oh.x, ol.x);
+            rb[1] = make_float4(eh.y, el.y, oh.y, ol.y);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(redfull);  // after this warp's T_{k+1} stores of the tile
+        const int rw = warp - kRedWarps * (i % (kPipeCW / kRedWarps));
+        if (rw >= 0 && rw < kRedWarps) {
+            // this tile's reducers: (column, which) pairs summed over the
+            // consumer warps in warp order
+            if (wait_phase(redfull, (uint32_t)i & 1u, s_abort, a.err)) {
+                const int q = rw * 32 + lane, j = q >> 1, which = q & 1;
                 float hsum = 0.f, lsum = 0.f;
 #pragma unroll
                 for (int w = 0; w < kPipeCW; w++) {
@@ -424,11 +446,18 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                 a.partial[(((int64_t)(k - a.k0) * a.G + g) * a.B + chunk * kPipeCols + j) * 2 + which] =
                     make_float2(hsum, lsum);
             }
-        }
-        if (a.flags && tid == 0) {  // hand the tile to the publisher (also on abort: it returns)
-            const int ps = i % kPubSlots;
-            if (i < kPubSlots || wait_phase(&pubfree[ps], (uint32_t)((i / kPubSlots) - 1) & 1u, s_abort, a.err))
-                mbar_arrive(&pub[ps]);
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(redfree);
+                // the first reducer hands the tile to the publisher: it has seen every
+                // consumer warp's arrival, so all stores of the tile precede this
+                if (a.flags && rw == 0) {
+                    const int ps = i % kPubSlots;
+                    if (i < kPubSlots ||
+                        wait_phase(&pubfree[ps], (uint32_t)((i / kPubSlots) - 1) & 1u, s_abort, a.err))
+                        mbar_arrive(&pub[ps]);
+                }
+            }
         }
     }
 }
@@ -482,7 +511,7 @@ size_t cheb_f32_pipe_stage_bytes(int R, int maxU, int maxBlk, int rec_cap)
 size_t cheb_f32_pipe_smem(size_t stage_bytes, int stages)
 {
     return (size_t)stages * stage_bytes + (size_t)kPipeCW * kPipeCols * 4 * sizeof(float) +
-           (size_t)(2 * stages + 2 * kPubSlots) * sizeof(uint64_t) + 16;
+           (size_t)(2 * stages + 2 * kPubSlots + 2) * sizeof(uint64_t) + 16;
 }
 
 int cheb_f32_pipe_max_rows() { return kPipeCW * 3; }
