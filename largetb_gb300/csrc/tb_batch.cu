@@ -27,6 +27,7 @@
 #include <string>
 #include <vector>
 
+#include "tb_f32x2.cuh"
 #include "tb_internal.h"
 
 namespace tb {
@@ -177,18 +178,6 @@ __global__ void k_bt_identity(const Unit *__restrict__ units, int nunits, const 
     }
 }
 
-// (s, c) += x with the rounding error of s + x kept exactly in c (Knuth's
-// TwoSum): column dot products accumulate as FP32 pairs, since GB300 issues
-// FP64 at only about 2 operations per clock per SM.
-__device__ __forceinline__ void pair_add(float &s, float &c, float x)
-{
-    const float t = s + x;
-    const float bp = t - s;
-    const float e = (s - (t - bp)) + (x - bp);
-    s = t;
-    c += e;
-}
-
 // ---- one FP32 Chebyshev step for every unit (staged as k_cheb_f32_staged) ----
 __global__ void __launch_bounds__(32 * kBtWarps)
     k_bt_cheb_f32(const Unit *__restrict__ units, const int32_t *__restrict__ s_ao,
@@ -235,59 +224,39 @@ __global__ void __launch_bounds__(32 * kBtWarps)
     cpa_wait();
     __syncthreads();
     const int lane = tid & 31, w = tid >> 5, c = 2 * lane;
-    // pairs (hi, lo): <T_k,T_k> and <T_k,T_{k+1}> of columns c and c+1
-    float hs[4] = {0.f, 0.f, 0.f, 0.f}, ls[4] = {0.f, 0.f, 0.f, 0.f};
+    // pairs (hi, lo) packed over columns (c, c+1): <T_k,T_k> in (eh, el), <T_k,T_{k+1}> in (oh, ol)
+    float2 eh = make_float2(0.f, 0.f), el = eh, oh = eh, ol = eh;
     for (int r = w; r < nr; r += kBtWarps) {
         const int I = I0 + r;
-        float acc[4][2];
+        float2 acc[4];  // row q of the block row, columns (c, c+1)
 #pragma unroll
-        for (int q = 0; q < 4; q++) acc[q][0] = acc[q][1] = 0.f;
+        for (int q = 0; q < 4; q++) acc[q] = make_float2(0.f, 0.f);
         for (int t = sR[r]; t < sR[r + 1]; t++) {
             const float *tv = sT + sL[t] * 4 * kBtCols + c;
-            const float4 *xb = reinterpret_cast<const float4 *>(sX + t * 16);
             float2 v[4];
 #pragma unroll
             for (int m = 0; m < 4; m++) v[m] = *reinterpret_cast<const float2 *>(tv + m * kBtCols);
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const float4 xr = xb[q];
-                const float xm[4] = {xr.x, xr.y, xr.z, xr.w};
-#pragma unroll
-                for (int m = 0; m < 4; m++) {
-                    acc[q][0] = fmaf(xm[m], v[m].x, acc[q][0]);
-                    acc[q][1] = fmaf(xm[m], v[m].y, acc[q][1]);
-                }
-            }
+            block_fma2(acc, reinterpret_cast<const float4 *>(sX + t * 16), v);
         }
         const float *own = sT + lself[I] * 4 * kBtCols + c;
-        float ee[2] = {0.f, 0.f}, eo[2] = {0.f, 0.f};
+        float2 ee = make_float2(0.f, 0.f), eo = ee;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const float2 ov = *reinterpret_cast<const float2 *>(own + q * kBtCols);
-            float2 o;
-            if (first) {
-                o = make_float2(acc[q][0], acc[q][1]);
-            } else {
-                const float2 p = *reinterpret_cast<const float2 *>(sP + (r * 4 + q) * kBtCols + c);
-                o.x = 2.f * acc[q][0] - p.x;
-                o.y = 2.f * acc[q][1] - p.y;
-            }
+            float2 o = acc[q];
+            if (!first) o = cheb_next2(acc[q], *reinterpret_cast<const float2 *>(sP + (r * 4 + q) * kBtCols + c));
             *reinterpret_cast<float2 *>(Tout + (int64_t)(4 * (I - ao) + q) * B + col0 + c) = o;
-            ee[0] = fmaf(ov.x, ov.x, ee[0]);
-            ee[1] = fmaf(ov.y, ov.y, ee[1]);
-            eo[0] = fmaf(ov.x, o.x, eo[0]);
-            eo[1] = fmaf(ov.y, o.y, eo[1]);
+            ee = __ffma2_rn(ov, ov, ee);
+            eo = __ffma2_rn(ov, o, eo);
         }
-        pair_add(hs[0], ls[0], ee[0]);
-        pair_add(hs[1], ls[1], eo[0]);
-        pair_add(hs[2], ls[2], ee[1]);
-        pair_add(hs[3], ls[3], eo[1]);
+        pair_add2(eh, el, ee);
+        pair_add2(oh, ol, eo);
     }
     __syncthreads();
     float *red = reinterpret_cast<float *>(bsm4);  // [warp][col][which][hi, lo]
     float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)w * kBtCols + c) * 4);
-    rb[0] = make_float4(hs[0], ls[0], hs[1], ls[1]);
-    rb[1] = make_float4(hs[2], ls[2], hs[3], ls[3]);
+    rb[0] = make_float4(eh.x, el.x, oh.x, ol.x);
+    rb[1] = make_float4(eh.y, el.y, oh.y, ol.y);
     __syncthreads();
     if (tid < 2 * kBtCols) {
         const int j = tid >> 1, which = tid & 1;

@@ -28,6 +28,7 @@
 
 #include <algorithm>
 
+#include "tb_f32x2.cuh"
 #include "tb_internal.h"
 
 namespace tb {
@@ -311,18 +312,9 @@ void launch_cheb_step_f64(cudaStream_t st, const DevMatrix &m, const double *Tin
                                                 B, c0, first, d, kout);
 }
 
-// (s, c) += x with the rounding error of s + x kept exactly in c (Knuth's
-// TwoSum).  The FP32 step kernels accumulate their column dot products as
-// such FP32 pairs across block rows and warps and write (hi, lo) pairs; GB300
-// issues FP64 at only about 2 operations per clock per SM.
-__device__ __forceinline__ void pair_add(float &s, float &c, float x)
-{
-    const float t = s + x;
-    const float bp = t - s;
-    const float e = (s - (t - bp)) + (x - bp);
-    s = t;
-    c += e;
-}
+// The FP32 step kernels accumulate their column dot products as FP32 TwoSum
+// pairs (pair_add, tb_f32x2.cuh) across block rows and warps and write
+// (hi, lo) pairs.
 
 // ---------------------------------------------------------------------------
 // FP32 Chebyshev step with fused column dot products.
@@ -516,59 +508,40 @@ __global__ void __launch_bounds__(32 * kV2Warps)
     __syncthreads();
     // ---- compute ----
     const int lane = tid & 31, w = tid >> 5, c = 2 * lane;
-    float hs[4] = {0.f, 0.f, 0.f, 0.f}, ls[4] = {0.f, 0.f, 0.f, 0.f};  // ee c, eo c, ee c+1, eo c+1
+    // pairs (hi, lo) packed over columns (c, c+1): <T_k,T_k> in (eh, el), <T_k,T_{k+1}> in (oh, ol)
+    float2 eh = make_float2(0.f, 0.f), el = eh, oh = eh, ol = eh;
     for (int r = w; r < nr; r += kV2Warps) {
         const int I = I0 + r;
         const int ta = sR[r], te = sR[r + 1];
-        float acc[4][2];
+        float2 acc[4];  // row q of the block row, columns (c, c+1)
 #pragma unroll
-        for (int q = 0; q < 4; q++) acc[q][0] = acc[q][1] = 0.f;
+        for (int q = 0; q < 4; q++) acc[q] = make_float2(0.f, 0.f);
         for (int t = ta; t < te; t++) {
             const float *tv = sT + sL[t] * 4 * kV2Cols + c;
-            const float4 *xb = reinterpret_cast<const float4 *>(sX + t * 16);
             float2 v[4];
 #pragma unroll
             for (int m = 0; m < 4; m++) v[m] = *reinterpret_cast<const float2 *>(tv + m * kV2Cols);
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const float4 xr = xb[q];
-                const float xm[4] = {xr.x, xr.y, xr.z, xr.w};
-#pragma unroll
-                for (int m = 0; m < 4; m++) {
-                    acc[q][0] = fmaf(xm[m], v[m].x, acc[q][0]);
-                    acc[q][1] = fmaf(xm[m], v[m].y, acc[q][1]);
-                }
-            }
+            block_fma2(acc, reinterpret_cast<const float4 *>(sX + t * 16), v);
         }
         const float *own = sT + lself[I] * 4 * kV2Cols + c;
-        float ee[2] = {0.f, 0.f}, eo[2] = {0.f, 0.f};
+        float2 ee = make_float2(0.f, 0.f), eo = ee;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const float2 ov = *reinterpret_cast<const float2 *>(own + q * kV2Cols);
-            float2 o;
-            if (first) {
-                o = make_float2(acc[q][0], acc[q][1]);
-            } else {
-                const float2 p = *reinterpret_cast<const float2 *>(sP + (r * 4 + q) * kV2Cols + c);
-                o.x = 2.f * acc[q][0] - p.x;
-                o.y = 2.f * acc[q][1] - p.y;
-            }
+            float2 o = acc[q];
+            if (!first) o = cheb_next2(acc[q], *reinterpret_cast<const float2 *>(sP + (r * 4 + q) * kV2Cols + c));
             *reinterpret_cast<float2 *>(Tout + (int64_t)(4 * I + q) * B + col0 + c) = o;
-            ee[0] = fmaf(ov.x, ov.x, ee[0]);
-            ee[1] = fmaf(ov.y, ov.y, ee[1]);
-            eo[0] = fmaf(ov.x, o.x, eo[0]);
-            eo[1] = fmaf(ov.y, o.y, eo[1]);
+            ee = __ffma2_rn(ov, ov, ee);
+            eo = __ffma2_rn(ov, o, eo);
         }
-        pair_add(hs[0], ls[0], ee[0]);
-        pair_add(hs[1], ls[1], eo[0]);
-        pair_add(hs[2], ls[2], ee[1]);
-        pair_add(hs[3], ls[3], eo[1]);
+        pair_add2(eh, el, ee);
+        pair_add2(oh, ol, eo);
     }
     __syncthreads();  // shared T no longer needed: reuse for the reduction
     float *red = reinterpret_cast<float *>(smem4);  // [8][64][2 sums][hi, lo]
     float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)w * kV2Cols + c) * 4);
-    rb[0] = make_float4(hs[0], ls[0], hs[1], ls[1]);
-    rb[1] = make_float4(hs[2], ls[2], hs[3], ls[3]);
+    rb[0] = make_float4(eh.x, el.x, oh.x, ol.x);
+    rb[1] = make_float4(eh.y, el.y, oh.y, ol.y);
     __syncthreads();
     if (tid < 2 * kV2Cols) {
         const int j = tid >> 1, which = tid & 1;
@@ -690,11 +663,11 @@ __global__ void __launch_bounds__(32 * kPWarps, (kRPW <= 4 ? 3 : 2))
         float *Gn = (k & 1) ? G0 : G1;
         // ---- 1. contributions of the own rows (in shared memory already),
         // computed before waiting so the wait overlaps with work ----
-        float acc[kRPW][4][2];
+        float2 acc[kRPW][4];  // row q of the warp's j-th block row, columns (cl, cl+1)
 #pragma unroll
         for (int j = 0; j < kRPW; j++)
 #pragma unroll
-            for (int q = 0; q < 4; q++) acc[j][q][0] = acc[j][q][1] = 0.f;
+            for (int q = 0; q < 4; q++) acc[j][q] = make_float2(0.f, 0.f);
 #pragma unroll
         for (int j = 0; j < kRPW; j++) {
             const int r = w + j * kPWarps;
@@ -703,20 +676,10 @@ __global__ void __launch_bounds__(32 * kPWarps, (kRPW <= 4 ? 3 : 2))
                 const int code = sL[t];
                 if (code >= R) continue;
                 const float *tv = cur + code * rowf + cl;
-                const float4 *xb = reinterpret_cast<const float4 *>(sX + t * 16);
                 float2 v[4];
 #pragma unroll
                 for (int m = 0; m < 4; m++) v[m] = *reinterpret_cast<const float2 *>(tv + m * kPCols);
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const float4 xr = xb[q];
-                    const float xm[4] = {xr.x, xr.y, xr.z, xr.w};
-#pragma unroll
-                    for (int m = 0; m < 4; m++) {
-                        acc[j][q][0] = fmaf(xm[m], v[m].x, acc[j][q][0]);
-                        acc[j][q][1] = fmaf(xm[m], v[m].y, acc[j][q][1]);
-                    }
-                }
+                block_fma2(acc[j], reinterpret_cast<const float4 *>(sX + t * 16), v);
             }
         }
         // ---- 2. wait for the neighbours' step k: warp 0, one lane per
@@ -767,7 +730,8 @@ __global__ void __launch_bounds__(32 * kPWarps, (kRPW <= 4 ? 3 : 2))
         cp_async_wait_all();
         __syncthreads();
         // ---- 4. halo contributions, T_{k+1} for the own rows, dot products ----
-        float hs[4] = {0.f, 0.f, 0.f, 0.f}, ls[4] = {0.f, 0.f, 0.f, 0.f};  // ee c, eo c, ee c+1, eo c+1
+        // pairs (hi, lo) over columns (cl, cl+1): <T_k,T_k> in (eh, el), <T_k,T_{k+1}> in (oh, ol)
+        float2 eh = make_float2(0.f, 0.f), el = eh, oh = eh, ol = eh;
 #pragma unroll
         for (int j = 0; j < kRPW; j++) {
             const int r = w + j * kPWarps;
@@ -776,45 +740,24 @@ __global__ void __launch_bounds__(32 * kPWarps, (kRPW <= 4 ? 3 : 2))
                 const int code = sL[t];
                 if (code < R) continue;
                 const float *tv = halo + (code - R) * rowf + cl;
-                const float4 *xb = reinterpret_cast<const float4 *>(sX + t * 16);
                 float2 v[4];
 #pragma unroll
                 for (int m = 0; m < 4; m++) v[m] = *reinterpret_cast<const float2 *>(tv + m * kPCols);
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const float4 xr = xb[q];
-                    const float xm[4] = {xr.x, xr.y, xr.z, xr.w};
-#pragma unroll
-                    for (int m = 0; m < 4; m++) {
-                        acc[j][q][0] = fmaf(xm[m], v[m].x, acc[j][q][0]);
-                        acc[j][q][1] = fmaf(xm[m], v[m].y, acc[j][q][1]);
-                    }
-                }
+                block_fma2(acc[j], reinterpret_cast<const float4 *>(sX + t * 16), v);
             }
-            float ee[2] = {0.f, 0.f}, eo[2] = {0.f, 0.f};
+            float2 ee = make_float2(0.f, 0.f), eo = ee;
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const float2 ov = *reinterpret_cast<const float2 *>(cur + r * rowf + q * kPCols + cl);
                 float2 *pv = reinterpret_cast<float2 *>(prev + r * rowf + q * kPCols + cl);
-                float2 o;
-                if (k == 0) {
-                    o = make_float2(acc[j][q][0], acc[j][q][1]);
-                } else {
-                    const float2 p = *pv;
-                    o.x = 2.f * acc[j][q][0] - p.x;
-                    o.y = 2.f * acc[j][q][1] - p.y;
-                }
+                const float2 o = k == 0 ? acc[j][q] : cheb_next2(acc[j][q], *pv);
                 *pv = o;
                 *reinterpret_cast<float2 *>(Gn + (int64_t)(4 * (I0 + r) + q) * B + col0 + cl) = o;
-                ee[0] = fmaf(ov.x, ov.x, ee[0]);
-                ee[1] = fmaf(ov.y, ov.y, ee[1]);
-                eo[0] = fmaf(ov.x, o.x, eo[0]);
-                eo[1] = fmaf(ov.y, o.y, eo[1]);
+                ee = __ffma2_rn(ov, ov, ee);
+                eo = __ffma2_rn(ov, o, eo);
             }
-            pair_add(hs[0], ls[0], ee[0]);
-            pair_add(hs[1], ls[1], eo[0]);
-            pair_add(hs[2], ls[2], ee[1]);
-            pair_add(hs[3], ls[3], eo[1]);
+            pair_add2(eh, el, ee);
+            pair_add2(oh, ol, eo);
         }
         // ---- publish T_{k+1} ----
         __threadfence();
@@ -823,8 +766,8 @@ __global__ void __launch_bounds__(32 * kPWarps, (kRPW <= 4 ? 3 : 2))
         // ---- per-column partial sums (the halo buffer is free now) ----
         float *red = halo;  // [warps][64][2 sums][hi, lo]
         float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)w * kPCols + cl) * 4);
-        rb[0] = make_float4(hs[0], ls[0], hs[1], ls[1]);
-        rb[1] = make_float4(hs[2], ls[2], hs[3], ls[3]);
+        rb[0] = make_float4(eh.x, el.x, oh.x, ol.x);
+        rb[1] = make_float4(eh.y, el.y, oh.y, ol.y);
         __syncthreads();
         if (tid < 2 * kPCols) {
             const int j = tid >> 1, which = tid & 1;

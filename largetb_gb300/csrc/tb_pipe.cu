@@ -56,6 +56,7 @@
 
 #include <algorithm>
 
+#include "tb_f32x2.cuh"
 #include "tb_internal.h"
 
 namespace tb {
@@ -148,28 +149,6 @@ __device__ __forceinline__ void st_release(int32_t *p, int v)
 __device__ __forceinline__ void fence_proxy_async_global()
 {
     asm volatile("fence.proxy.async.global;\n" ::: "memory");
-}
-
-// (s, c) += x with the rounding error of s + x kept exactly in c (TwoSum)
-__device__ __forceinline__ void pair_add(float &s, float &c, float x)
-{
-    const float t = s + x;
-    const float bp = t - s;
-    const float e = (s - (t - bp)) + (x - bp);
-    s = t;
-    c += e;
-}
-
-// pair_add on both components of packed FP32 pairs; fma(-1, a, b) is b - a
-// with the same single rounding
-__device__ __forceinline__ void pair_add2(float2 &s, float2 &c, float2 x)
-{
-    const float2 m1 = make_float2(-1.f, -1.f);
-    const float2 t = __fadd2_rn(s, x);
-    const float2 bp = __ffma2_rn(m1, s, t);
-    const float2 e = __fadd2_rn(__ffma2_rn(m1, __ffma2_rn(m1, bp, t), s), __ffma2_rn(m1, bp, x));
-    s = t;
-    c = __fadd2_rn(c, e);
 }
 
 // Poll until the phase of the given parity completes; false on abort or
@@ -376,9 +355,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
             const int32_t *sLc = sRp + nr + 1;
             const int32_t *sLs = sLc + sRp[nr];
             for (int r = warp; r < nr; r += kPipeCW) {
-                // acc[q] = row q of the block row, columns (c, c+1): packed
-                // FP32 pairs, one fma.f32x2 per (q, m), each component
-                // rounded exactly as fmaf
+                // acc[q] = row q of the block row, columns (c, c+1)
                 float2 acc[4];
 #pragma unroll
                 for (int q = 0; q < 4; q++) acc[q] = make_float2(0.f, 0.f);
@@ -389,14 +366,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                     float2 v[4];
 #pragma unroll
                     for (int m = 0; m < 4; m++) v[m] = *reinterpret_cast<const float2 *>(tv + m * kPipeCols);
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const float4 xr = xb[q];
-                        acc[q] = __ffma2_rn(make_float2(xr.x, xr.x), v[0], acc[q]);
-                        acc[q] = __ffma2_rn(make_float2(xr.y, xr.y), v[1], acc[q]);
-                        acc[q] = __ffma2_rn(make_float2(xr.z, xr.z), v[2], acc[q]);
-                        acc[q] = __ffma2_rn(make_float2(xr.w, xr.w), v[3], acc[q]);
-                    }
+                    block_fma2(acc, xb, v);
                 }
                 const float *own = sT + sLs[r] * 4 * kPipeCols + c;
                 float2 ee = make_float2(0.f, 0.f), eo = ee;
@@ -404,10 +374,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                 for (int q = 0; q < 4; q++) {
                     const float2 ov = *reinterpret_cast<const float2 *>(own + q * kPipeCols);
                     float2 o = acc[q];
-                    if (k > 0) {  // 2 acc - p: exact doubling, then fma(-1, p, 2 acc) rounds once
-                        const float2 p = *reinterpret_cast<const float2 *>(sP + (r * 4 + q) * kPipeCols + c);
-                        o = __ffma2_rn(make_float2(-1.f, -1.f), p, __fadd2_rn(acc[q], acc[q]));
-                    }
+                    if (k > 0) o = cheb_next2(acc[q], *reinterpret_cast<const float2 *>(sP + (r * 4 + q) * kPipeCols + c));
                     *reinterpret_cast<float2 *>(out + (r * 4 + q) * kPipeCols) = o;
                     ee = __ffma2_rn(ov, ov, ee);
                     eo = __ffma2_rn(ov, o, eo);

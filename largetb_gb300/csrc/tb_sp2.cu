@@ -24,6 +24,7 @@
 #include <cstring>
 #include <vector>
 
+#include "tb_f32x2.cuh"
 #include "tb_internal.h"
 
 namespace tb {
@@ -65,16 +66,6 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total)
     *total = sh[kSp2Threads / 32 - 1];
     __syncthreads();
     return before;
-}
-
-// (s, c) += x with the rounding error of s + x kept exactly in c (TwoSum)
-__device__ __forceinline__ void pair_add(float &s, float &c, float x)
-{
-    const float t = s + x;
-    const float bp = t - s;
-    const float e = (s - (t - bp)) + (x - bp);
-    s = t;
-    c += e;
 }
 
 __device__ __forceinline__ double warp_sum_d(double v)
