@@ -322,6 +322,51 @@ def run_sp2_bench(args, T, dev, rank):
                           "max_dq_fp32_vs_fp64": dq}), flush=True)
 
 
+def run_all_kernels(T, dev):
+    """Every kernel of the library once or a few times on small inputs: the
+    program behind the per-kernel launch list (duration and DRAM traffic of
+    each kernel under ncu).  Prints one JSON line naming the calls made."""
+    from largetb_gb300 import learned
+    m = T.model_cristobalite(3, 3, 3, sigma_ang=0.05, seed=7)
+    calls = []
+    for kern in (T.FP32_STAGED, T.FP32_PERSISTENT, T.FP32_PIPELINED, T.FP32_PIPELINED_STEP):
+        with T.Context(M=60, precision=T.PREC_FP32, fp32_kernel=kern, device=dev,
+                       column_block=0 if kern == T.FP32_PERSISTENT else 512) as c:
+            c.set_model(m)
+            c.density()
+        calls.append(f"density fp32 kernel {kern}")
+    with T.Context(M=60, precision=T.PREC_FP64, scc_max_iter=2, device=dev) as c:
+        c.set_model(m)
+        c.scc_solve(raise_on_cap=False)
+        c.kpm_dos(n_moments=60, n_random=8, seed=1, npts=120)
+    calls += ["scc fp64 x2", "kpm_dos"]
+    with T.Context(M=60, precision=T.PREC_FP32, check_fp32=1, fp32_kernel=T.FP32_PIPELINED_STEP,
+                   column_block=512, scc_max_iter=3, device=dev) as c:
+        c.set_model(m)
+        c.density()
+        c.scc_solve(raise_on_cap=False)
+    calls += ["density fp32 + fp64 check", "scc fp32 x3 (graph)"]
+    with T.Context(precision=T.PREC_FP32, sp2_max_iter=6, device=dev) as c:
+        c.set_model(T.model_cristobalite(2, 2, 2, sigma_ang=0.08, seed=3))
+        c.sp2()
+    calls.append("sp2 x6")
+    with T.Context(M=60, device=dev) as c:
+        c.set_geometry(m.xyz, m.species, learned.cell_box((3, 3, 3)), rcut_bohr=4.0, gamma_diag=1.0)
+        c.density()
+    calls.append("set_geometry + density")
+    with T.Batch([T.model_cristobalite(*d, sigma_ang=0.05, seed=i)
+                  for i, d in enumerate([(1, 1, 2), (2, 1, 2), (2, 2, 2)])], M=60, device=dev) as b:
+        b.scc_solve()
+    calls.append("batch of 3")
+    X = T.mlp_features(m.xyz, m.species, learned.cell_box((3, 3, 3)))
+    mlp = T.MLP(device=dev, seed=2)
+    mlp.train(X, np.zeros(len(X), np.float32), epochs=1, batch=256, lr=1e-3)
+    mlp.predict(X)
+    mlp.predict_fp32(X)
+    calls += ["mlp train 1 epoch", "mlp predict (tensor cores)", "mlp predict fp32"]
+    print(json.dumps({"all_kernels": calls}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -345,6 +390,8 @@ def main():
                     help="64 cristobalite cells of random shape solved as one batch (M = 300)")
     ap.add_argument("--sp2", action="store_true",
                     help="time SP2 purification of 4x4x4 cristobalite (sigma 0.08 A, drop 1e-5)")
+    ap.add_argument("--all-kernels", action="store_true",
+                    help="run every kernel of the library on small inputs (for the ncu launch list)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -356,6 +403,9 @@ def main():
     T.load()
     dev = local
     torch.cuda.set_device(dev)
+    if args.all_kernels:
+        run_all_kernels(T, dev)
+        return
     if args.sp2:
         run_sp2_bench(args, T, dev, rank)
         return
