@@ -406,6 +406,9 @@ int ensure_work(tb_ctx *ctx)
     TB_TRY(dalloc(ctx, w.mom, (size_t)M + 1));
     TB_TRY(dalloc(ctx, w.c, (size_t)M));
     TB_TRY(dalloc(ctx, w.rho, (size_t)w.nq_cap));
+    TB_TRY(dalloc(ctx, w.fq, (size_t)w.nq_cap));
+    TB_TRY(dalloc(ctx, w.costab, 4 * (size_t)w.nq_cap));
+    launch_cos_table(ctx->stream, w.nq_cap, w.costab);
     TB_TRY(dalloc(ctx, w.cand, (size_t)kBisectCand));
     TB_TRY(dalloc(ctx, w.diagP, (size_t)m.n));
     TB_TRY(dalloc(ctx, w.q, (size_t)m.natoms));
@@ -855,17 +858,17 @@ int density_eval(tb_ctx *ctx, bool have_shift)
     launch_moment_sums(st, w.d, m.n, M + 1, w.mom);
     ctx->launches++;
     if (p.kT > 0) {
-        launch_dos_nodes(st, w.g, w.mom, M, w.state, w.nq_cap, w.rho);
+        launch_dos_nodes(st, w.g, w.mom, M, w.state, w.nq_cap, w.costab, w.rho);
         ctx->launches++;
     }
     for (int r = 0; r < kBisectRounds; r++) {
-        launch_bisect_round(st, w.rho, w.g, w.mom, M, ctx->p.n_electrons, p.mu_tol, r, w.cand,
-                            w.state);
+        launch_bisect_round(st, w.rho, w.g, w.mom, w.costab, w.nq_cap, M, ctx->p.n_electrons, p.mu_tol, r,
+                            w.cand, w.state);
         ctx->launches++;
     }
-    launch_fermi_coeffs(st, M, w.state, w.c);
+    launch_fermi_coeffs(st, M, w.state, w.nq_cap, w.costab, w.fq, w.c);
     launch_charges(st, w.d, w.c, w.g, w.mom, M, m.n, m.natoms, w.diagP, w.q, w.state);
-    ctx->launches += 3;
+    ctx->launches += 4;
     TB_CUDA(cudaGetLastError());
     return TB_OK;
 }
@@ -1095,6 +1098,8 @@ void free_all(tb_ctx *ctx)
     dfree(w.g);
     dfree(w.c);
     dfree(w.rho);
+    dfree(w.fq);
+    dfree(w.costab);
     dfree(w.cand);
     dfree(w.diagP);
     dfree(w.q);

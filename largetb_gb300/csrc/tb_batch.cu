@@ -310,24 +310,51 @@ __global__ void __launch_bounds__(256)
     if (threadIdx.x == 0) mom[(int64_t)s * (M + 1) + k] = v;
 }
 
+// Node kernels index the cosine table of k_cos_table (tab[j] = cos(pi j /
+// (2 nq_cap))): cos(theta_q) = tab[(2q+1) r], cos(k theta_q) = tab[(k (2q+1)
+// mod 4 nq) r], r = nq > 0 ? nq_cap / nq : 1, as in the single-structure kernels.
 __global__ void k_bt_dos_nodes(const double *__restrict__ g, const double *__restrict__ mom, int M,
                                const DevState *__restrict__ st, const int32_t *__restrict__ active,
-                               int nq_cap, double *__restrict__ rho)
+                               int nq_cap, const double *__restrict__ tab, double *__restrict__ rho)
 {
+    extern __shared__ double wk[];  // (2 - delta_k0) g_k mu_k of this structure
     const int s = blockIdx.y;
     if (!active[s]) return;
-    const int nq = st[s].nq;
     const double *ms = mom + (int64_t)s * (M + 1);
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq && q < nq_cap; q += gridDim.x * blockDim.x) {
-        const double th = kPi * (q + 0.5) / nq;
-        double v = g[0] * ms[0];
-        for (int kk = 1; kk < M; kk++) v += 2.0 * g[kk] * ms[kk] * cos(kk * th);
+    for (int kk = threadIdx.x; kk < M; kk += blockDim.x) wk[kk] = kk == 0 ? g[0] * ms[0] : 2.0 * g[kk] * ms[kk];
+    __syncthreads();
+    const int nq = min(st[s].nq, nq_cap), r = nq > 0 ? nq_cap / nq : 1;
+    const size_t cmask = 4 * (size_t)nq_cap - 1;  // keeps every table index in range
+    const unsigned mask = 4u * (unsigned)nq - 1u;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const unsigned step = 2u * (unsigned)q + 1u;
+        unsigned j = 0;
+        double v = wk[0];
+        for (int kk = 1; kk < M; kk++) {
+            j = (j + step) & mask;
+            v += wk[kk] * tab[((size_t)j * r) & cmask];
+        }
         rho[(int64_t)s * nq_cap + q] = v;
     }
 }
 
+__global__ void k_bt_fermi_nodes(const DevState *__restrict__ st_all, const int32_t *__restrict__ active,
+                                 int nq_cap, const double *__restrict__ tab, double *__restrict__ fq)
+{
+    const int s = blockIdx.y;
+    if (!active[s]) return;
+    const DevState *st = st_all + s;
+    const double beta = st->beta_x, mu = st->mu_x;
+    if (!(beta > 0)) return;
+    const int nq = min(st->nq, nq_cap), r = nq > 0 ? nq_cap / nq : 1;
+    const size_t cmask = 4 * (size_t)nq_cap - 1;  // keeps every table index in range
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x)
+        fq[(int64_t)s * nq_cap + q] = fermi_d(tab[((size_t)(2 * q + 1) * r) & cmask], mu, beta);
+}
+
 __global__ void __launch_bounds__(256)
-    k_bt_bisect(const double *__restrict__ rho, int nq_cap, const double *__restrict__ g,
+    k_bt_bisect(const double *__restrict__ rho, int nq_cap, const double *__restrict__ tab,
+                const double *__restrict__ g,
                 const double *__restrict__ mom, int M, const double *__restrict__ n_elec, double tol_n,
                 int round, int last_round, const int32_t *__restrict__ active, double *__restrict__ cand,
                 DevState *__restrict__ st_all)
@@ -342,9 +369,11 @@ __global__ void __launch_bounds__(256)
     const double *ms = mom + (int64_t)s * (M + 1);
     double v = 0.0;
     if (beta > 0) {
-        const int nq = st->nq;
+        const int nq = st->nq, r = nq > 0 ? nq_cap / nq : 1;
+        const size_t cmask = 4 * (size_t)nq_cap - 1;  // keeps every table index in range
         const double *rs = rho + (int64_t)s * nq_cap;
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) v += fermi_d(cos(kPi * (q + 0.5) / nq), mu, beta) * rs[q];
+        for (int q = threadIdx.x; q < nq; q += blockDim.x)
+            v += fermi_d(tab[((size_t)(2 * q + 1) * r) & cmask], mu, beta) * rs[q];
         v = 2.0 * bsum(v, sh) / nq;
     } else {
         const double th = acos(mu);
@@ -399,8 +428,8 @@ __global__ void __launch_bounds__(256)
 }
 
 __global__ void __launch_bounds__(256)
-    k_bt_coeffs(int M, DevState *__restrict__ st_all, const int32_t *__restrict__ active,
-                double *__restrict__ c)
+    k_bt_coeffs(int M, DevState *__restrict__ st_all, const int32_t *__restrict__ active, int nq_cap,
+                const double *__restrict__ tab, const double *__restrict__ fq, double *__restrict__ c)
 {
     __shared__ double sh[32];
     const int k = blockIdx.x, s = blockIdx.y;
@@ -410,12 +439,13 @@ __global__ void __launch_bounds__(256)
     if (threadIdx.x == 0 && k == 0) st->mu = st->a * mu + st->b;
     double *cs = c + (int64_t)s * M;
     if (beta > 0) {
-        const int nq = st->nq;
+        const int nq = st->nq, r = nq > 0 ? nq_cap / nq : 1;
+        const size_t cmask = 4 * (size_t)nq_cap - 1;  // keeps every table index in range
+        const unsigned mask = 4u * (unsigned)nq - 1u;
+        const double *fs = fq + (int64_t)s * nq_cap;
         double v = 0.0;
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-            const double th = kPi * (q + 0.5) / nq;
-            v += fermi_d(cos(th), mu, beta) * cos(k * th);
-        }
+        for (int q = threadIdx.x; q < nq; q += blockDim.x)
+            v += fs[q] * tab[((size_t)(((unsigned)k * (2u * (unsigned)q + 1u)) & mask) * r) & cmask];
         v = bsum(v, sh);
         if (threadIdx.x == 0) cs[k] = (k == 0 ? 1.0 : 2.0) * v / nq;
     } else if (threadIdx.x == 0) {
@@ -662,6 +692,7 @@ struct tb_batch {
     int64_t *s_toff = nullptr, *s_poff = nullptr;
     double *h0 = nullptr, *h0diag = nullptr, *radius = nullptr, *d = nullptr, *mom = nullptr, *c = nullptr;
     double *g = nullptr, *rho = nullptr, *cand = nullptr, *diagP = nullptr, *q = nullptr, *partial = nullptr;
+    double *fq = nullptr, *costab = nullptr;  // Fermi function at the nodes [S][nq_cap]; cosine table 4 nq_cap
     double *g_v = nullptr, *q0d = nullptr, *qin = nullptr, *shift = nullptr, *hq = nullptr, *hr = nullptr;
     double *ne = nullptr;
     float *x32 = nullptr, *xdiag32 = nullptr, *T0 = nullptr, *T1 = nullptr;
@@ -839,6 +870,9 @@ int batch_build(tb_batch *b)
     BT(balloc(b, b->mom, (size_t)S * (M + 1)));
     BT(balloc(b, b->c, (size_t)S * M));
     BT(balloc(b, b->rho, (size_t)S * nq_cap));
+    BT(balloc(b, b->fq, (size_t)S * nq_cap));
+    BT(balloc(b, b->costab, 4 * (size_t)nq_cap));
+    launch_cos_table(b->stream, nq_cap, b->costab);
     BT(balloc(b, b->cand, (size_t)S * kBisectCand));
     BT(balloc(b, b->diagP, (size_t)n));
     BT(balloc(b, b->q, (size_t)na));
@@ -1046,12 +1080,14 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
             record(m1);
             k_bt_moment_sums<<<dim3(M + 1, S), 256, 0, st>>>(b->d, n, M, b->s_ao, b->active, b->mom);
             if (b->p.kT > 0)
-                k_bt_dos_nodes<<<dim3(64, S), 256, 0, st>>>(b->g, b->mom, M, b->st, b->active, b->nq_cap, b->rho);
+                k_bt_dos_nodes<<<dim3(64, S), 256, sizeof(double) * M, st>>>(b->g, b->mom, M, b->st, b->active,
+                                                                             b->nq_cap, b->costab, b->rho);
             for (int r = 0; r < kBisectRounds; r++)
-                k_bt_bisect<<<dim3(kBisectCand, S), 256, 0, st>>>(b->rho, b->nq_cap, b->g, b->mom, M, b->ne,
-                                                                  b->p.mu_tol, r, kBisectRounds - 1, b->active,
-                                                                  b->cand, b->st);
-            k_bt_coeffs<<<dim3(M, S), 256, 0, st>>>(M, b->st, b->active, b->c);
+                k_bt_bisect<<<dim3(kBisectCand, S), 256, 0, st>>>(b->rho, b->nq_cap, b->costab, b->g, b->mom, M,
+                                                                  b->ne, b->p.mu_tol, r, kBisectRounds - 1,
+                                                                  b->active, b->cand, b->st);
+            k_bt_fermi_nodes<<<dim3(16, S), 256, 0, st>>>(b->st, b->active, b->nq_cap, b->costab, b->fq);
+            k_bt_coeffs<<<dim3(M, S), 256, 0, st>>>(M, b->st, b->active, b->nq_cap, b->costab, b->fq, b->c);
             k_bt_charges<<<(na + 255) / 256, 256, 0, st>>>(b->d, b->c, b->g, M, n, na, b->s_of_atom, b->active,
                                                            b->diagP, b->q);
             k_bt_eband<<<S, 256, 0, st>>>(b->c, b->g, b->mom, M, b->active, b->st);
@@ -1087,7 +1123,7 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
         } else {
             issue();
         }
-        launches += 3 + 2 * (int64_t)K + 6 + kBisectRounds - (b->p.kT > 0 ? 0 : 1);
+        launches += 3 + 2 * (int64_t)K + 7 + kBisectRounds - (b->p.kT > 0 ? 0 : 1);
         spmm += K;
         // algorithmic bytes of a batched step: the sum over active structures
         // of nnzb_s (16 s + 4) + (nb_s + 1) 4 + 3 n_s B_s s, s = 4

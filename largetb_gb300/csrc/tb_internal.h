@@ -125,6 +125,8 @@ struct DevWork {
     double *g = nullptr;       // M damping factors
     double *c = nullptr;       // M expansion coefficients
     double *rho = nullptr;     // nq damped DOS at the quadrature nodes
+    double *fq = nullptr;      // nq Fermi function at the quadrature nodes
+    double *costab = nullptr;  // 4 nq_cap: cos(pi j / (2 nq_cap)), see k_cos_table
     double *cand = nullptr;    // kBisectCand electron counts
     double *diagP = nullptr;   // n
     double *q = nullptr;       // natoms
@@ -244,12 +246,14 @@ int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const Stage
                                 const float *Tin, float *Tout, int B, int first,
                                 float2 *partial_k);
 void launch_moment_sums(cudaStream_t st, const double *d, int n, int nmom, double *mom);
+void launch_cos_table(cudaStream_t st, int nq_cap, double *tab);
 void launch_dos_nodes(cudaStream_t st, const double *g, const double *mom, int M,
-                      const DevState *state, int nq_cap, double *rho);
+                      const DevState *state, int nq_cap, const double *tab, double *rho);
 void launch_bisect_round(cudaStream_t st, const double *rho, const double *g, const double *mom,
-                         int M, double n_elec, double tol_n, int round, double *cand,
-                         DevState *state);
-void launch_fermi_coeffs(cudaStream_t st, int M, DevState *state, double *c);
+                         const double *tab, int nq_cap, int M, double n_elec, double tol_n, int round,
+                         double *cand, DevState *state);
+void launch_fermi_coeffs(cudaStream_t st, int M, DevState *state, int nq_cap, const double *tab, double *fq,
+                         double *c);
 void launch_charges(cudaStream_t st, const double *d, const double *c, const double *g,
                     const double *mom, int M, int n, int natoms, double *diagP, double *q,
                     DevState *state);

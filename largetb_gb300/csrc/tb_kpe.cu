@@ -860,28 +860,58 @@ void launch_moment_sums(cudaStream_t st, const double *d, int n, int nmom, doubl
     k_moment_sums<<<nmom, 256, 0, st>>>(d, n, mom);
 }
 
+// tab[j] = cos(pi j / (2 nq_cap)), j < 4 nq_cap, built once per workspace.
+// For a quadrature of nq nodes (nq and nq_cap powers of two, r = nq > 0 ? nq_cap / nq : 1)
+// the nodes are theta_q = pi (2q+1) / (2 nq): cos(theta_q) is entry (2q+1) r
+// (the same double as cos(pi (q + 1/2) / nq): the arguments differ by exact
+// power-of-two scalings) and cos(k theta_q) is entry (k (2q+1) mod 4 nq) r;
+// the residue is a mask, also after 32-bit wrap-around.  The node kernels
+// below then evaluate no cosine per (k, q).
+__global__ void k_cos_table(int nq_cap, double *__restrict__ tab)
+{
+    const double h = kPi / (2.0 * nq_cap);
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 4 * nq_cap; j += gridDim.x * blockDim.x)
+        tab[j] = cos(h * j);
+}
+
+void launch_cos_table(cudaStream_t st, int nq_cap, double *tab)
+{
+    const int T = 256;
+    const int blocks = (int)std::min<int64_t>((4 * (int64_t)nq_cap + T - 1) / T, 1024);
+    k_cos_table<<<blocks, T, 0, st>>>(nq_cap, tab);
+}
+
 // rho_q = g_0 mu_0 + 2 sum_{k>=1} g_k mu_k cos(k theta_q): the damped DOS at
 // the Chebyshev-Gauss nodes (times pi sin theta), nq read from the state.
 __global__ void k_dos_nodes(const double *__restrict__ g, const double *__restrict__ mom, int M,
-                            const DevState *__restrict__ st, int nq_cap, double *__restrict__ rho)
+                            const DevState *__restrict__ st, int nq_cap, const double *__restrict__ tab,
+                            double *__restrict__ rho)
 {
-    const int nq = st->nq;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq && q < nq_cap;
-         q += gridDim.x * blockDim.x) {
-        const double th = kPi * (q + 0.5) / nq;
-        double s = g[0] * mom[0];
-        for (int k = 1; k < M; k++) s += 2.0 * g[k] * mom[k] * cos(k * th);
+    extern __shared__ double wk[];  // (2 - delta_k0) g_k mu_k
+    for (int k = threadIdx.x; k < M; k += blockDim.x) wk[k] = k == 0 ? g[0] * mom[0] : 2.0 * g[k] * mom[k];
+    __syncthreads();
+    const int nq = min(st->nq, nq_cap), r = nq > 0 ? nq_cap / nq : 1;
+    const size_t cmask = 4 * (size_t)nq_cap - 1;  // keeps every table index in range
+    const unsigned mask = 4u * (unsigned)nq - 1u;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const unsigned step = 2u * (unsigned)q + 1u;
+        unsigned j = 0;
+        double s = wk[0];
+        for (int k = 1; k < M; k++) {
+            j = (j + step) & mask;
+            s += wk[k] * tab[((size_t)j * r) & cmask];
+        }
         rho[q] = s;
     }
 }
 
 void launch_dos_nodes(cudaStream_t st, const double *g, const double *mom, int M,
-                            const DevState *state, int nq_cap, double *rho)
+                      const DevState *state, int nq_cap, const double *tab, double *rho)
 {
     const int T = 256;
     int blocks = (nq_cap + T - 1) / T;
     if (blocks > 1024) blocks = 1024;
-    k_dos_nodes<<<blocks, T, 0, st>>>(g, mom, M, state, nq_cap, rho);
+    k_dos_nodes<<<blocks, T, sizeof(double) * M, st>>>(g, mom, M, state, nq_cap, tab, rho);
 }
 
 // ---------------------------------------------------------------------------
@@ -891,8 +921,9 @@ void launch_dos_nodes(cudaStream_t st, const double *g, const double *mom, int M
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
     k_bisect_round(const double *__restrict__ rho, const double *__restrict__ g,
-                   const double *__restrict__ mom, int M, double n_elec, double tol_n, int round,
-                   int last_round, double *__restrict__ cand, DevState *st)
+                   const double *__restrict__ mom, const double *__restrict__ tab, int nq_cap, int M,
+                   double n_elec, double tol_n, int round, int last_round, double *__restrict__ cand,
+                   DevState *st)
 {
     __shared__ double sh[32];
     __shared__ int s_last;
@@ -904,10 +935,10 @@ __global__ void __launch_bounds__(256)
     double s = 0.0;
     if (beta_x > 0) {
         const int nq = st->nq;
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-            const double x = cos(kPi * (q + 0.5) / nq);
-            s += fermi(x, mu, beta_x) * rho[q];
-        }
+        const int r = nq > 0 ? nq_cap / nq : 1;
+        const size_t cmask = 4 * (size_t)nq_cap - 1;  // keeps every table index in range
+        for (int q = threadIdx.x; q < nq; q += blockDim.x)
+            s += fermi(tab[((size_t)(2 * q + 1) * r) & cmask], mu, beta_x) * rho[q];
         s = block_sum(s, sh);
         s = 2.0 * s / nq;
     } else {
@@ -970,27 +1001,42 @@ __global__ void __launch_bounds__(256)
 }
 
 void launch_bisect_round(cudaStream_t st, const double *rho, const double *g, const double *mom,
-                         int M, double n_elec, double tol_n, int round, double *cand,
-                         DevState *state)
+                         const double *tab, int nq_cap, int M, double n_elec, double tol_n, int round,
+                         double *cand, DevState *state)
 {
-    k_bisect_round<<<kBisectCand, 256, 0, st>>>(rho, g, mom, M, n_elec, tol_n, round,
+    k_bisect_round<<<kBisectCand, 256, 0, st>>>(rho, g, mom, tab, nq_cap, M, n_elec, tol_n, round,
                                                 kBisectRounds - 1, cand, state);
 }
 
+// f_q = Fermi function at the quadrature nodes for the final mu_x
+__global__ void k_fermi_nodes(const DevState *__restrict__ st, int nq_cap, const double *__restrict__ tab,
+                              double *__restrict__ fq)
+{
+    const double beta_x = st->beta_x;
+    if (!(beta_x > 0)) return;
+    const int nq = min(st->nq, nq_cap), r = nq > 0 ? nq_cap / nq : 1;
+    const size_t cmask = 4 * (size_t)nq_cap - 1;  // keeps every table index in range
+    const double mu_x = st->mu_x;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x)
+        fq[q] = fermi(tab[((size_t)(2 * q + 1) * r) & cmask], mu_x, beta_x);
+}
+
 // c_k(mu*) by Chebyshev-Gauss quadrature (FP64), or the step coefficients.
-__global__ void __launch_bounds__(256) k_fermi_coeffs(int M, DevState *st, double *__restrict__ c)
+__global__ void __launch_bounds__(256) k_fermi_coeffs(int M, DevState *st, const double *__restrict__ tab,
+                                                      int nq_cap, const double *__restrict__ fq,
+                                                      double *__restrict__ c)
 {
     __shared__ double sh[32];
     const int k = blockIdx.x;
     const double mu_x = st->mu_x, beta_x = st->beta_x;
     if (threadIdx.x == 0 && k == 0) st->mu = st->a * mu_x + st->b;
     if (beta_x > 0) {
-        const int nq = st->nq;
+        const int nq = st->nq, r = nq > 0 ? nq_cap / nq : 1;
+        const size_t cmask = 4 * (size_t)nq_cap - 1;  // keeps every table index in range
+        const unsigned mask = 4u * (unsigned)nq - 1u;
         double s = 0.0;
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-            const double th = kPi * (q + 0.5) / nq;
-            s += fermi(cos(th), mu_x, beta_x) * cos(k * th);
-        }
+        for (int q = threadIdx.x; q < nq; q += blockDim.x)
+            s += fq[q] * tab[((size_t)(((unsigned)k * (2u * (unsigned)q + 1u)) & mask) * r) & cmask];
         s = block_sum(s, sh);
         if (threadIdx.x == 0) c[k] = (k == 0 ? 1.0 : 2.0) * s / nq;
     } else if (threadIdx.x == 0) {
@@ -999,12 +1045,18 @@ __global__ void __launch_bounds__(256) k_fermi_coeffs(int M, DevState *st, doubl
     }
 }
 
-void launch_fermi_coeffs(cudaStream_t st, int M, DevState *state, double *c)
+void launch_fermi_coeffs(cudaStream_t st, int M, DevState *state, int nq_cap, const double *tab, double *fq,
+                         double *c)
 {
-    k_fermi_coeffs<<<M, 256, 0, st>>>(M, state, c);
+    const int T = 256;
+    const int blocks = std::min((nq_cap + T - 1) / T, 1024);
+    k_fermi_nodes<<<blocks, T, 0, st>>>(state, nq_cap, tab, fq);
+    k_fermi_coeffs<<<M, T, 0, st>>>(M, state, tab, nq_cap, fq, c);
 }
 
-// diagP_i = sum_k c_k g_k d[k][i];  q_a = 2 sum_{i in a} diagP_i.
+// diagP_i = sum_k c_k g_k d[k][i] (one thread per orbital, coalesced rows of
+// d);  q_a = 2 sum_{i in a} diagP_i over the atom's four consecutive orbitals
+// (lanes 4a' .. 4a'+3 of a warp, n = 4 natoms).
 __global__ void __launch_bounds__(256)
     k_charges(const double *__restrict__ d, const double *__restrict__ c,
               const double *__restrict__ g, int M, int n, int natoms, double *__restrict__ diagP,
@@ -1013,26 +1065,17 @@ __global__ void __launch_bounds__(256)
     extern __shared__ double wsh[];
     for (int k = threadIdx.x; k < M; k += blockDim.x) wsh[k] = c[k] * g[k];
     __syncthreads();
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= natoms) return;
-    double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
-    const double *base = d + 4 * (int64_t)a;
-    for (int k = 0; k < M; k++) {
-        const double w = wsh[k];
-        const double2 v0 = *reinterpret_cast<const double2 *>(base + (int64_t)k * n);
-        const double2 v1 = *reinterpret_cast<const double2 *>(base + (int64_t)k * n + 2);
-        p0 += w * v0.x;
-        p1 += w * v0.y;
-        p2 += w * v1.x;
-        p3 += w * v1.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double p = 0.0;
+    if (i < n) {
+#pragma unroll 8
+        for (int k = 0; k < M; k++) p += wsh[k] * d[(int64_t)k * n + i];
+        if (diagP) diagP[i] = p;
     }
-    if (diagP) {
-        diagP[4 * a + 0] = p0;
-        diagP[4 * a + 1] = p1;
-        diagP[4 * a + 2] = p2;
-        diagP[4 * a + 3] = p3;
-    }
-    q[a] = 2.0 * (p0 + p1 + p2 + p3);
+    // n is a multiple of 4 and blockDim.x of 32: an atom's orbitals share a warp
+    double s = p + __shfl_xor_sync(0xffffffffu, p, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (i < n && (i & 3) == 0) q[i >> 2] = 2.0 * s;
 }
 
 // n_found = 2 sum_k c_k g_k mu_k;  E_band = 2 sum_k c_k g_k (a tr(T_k X) + b mu_k).
@@ -1062,7 +1105,7 @@ void launch_charges(cudaStream_t st, const double *d, const double *c, const dou
                     DevState *state)
 {
     const int T = 256;
-    k_charges<<<(natoms + T - 1) / T, T, sizeof(double) * M, st>>>(d, c, g, M, n, natoms, diagP, q);
+    k_charges<<<(n + T - 1) / T, T, sizeof(double) * M, st>>>(d, c, g, M, n, natoms, diagP, q);
     k_eband<<<1, 256, 0, st>>>(c, g, mom, M, state);
 }
 
