@@ -40,11 +40,22 @@ struct Sp2Scalars {
 
 namespace {
 
-constexpr int kSp2Threads = 256;
+constexpr int kSp2Threads = 1024;  // 32 warps: the dense-row accumulator allows 2 CTAs per SM
+static_assert(kSp2Threads % 32 == 0 && kSp2Threads <= 1024, "SP2 block size");
+constexpr int kSp2ScanInts = 32;  // one int per warp for block_excl_scan
+constexpr int kSp2MiscInts = 8;   // [0] total, [1] overflow, [2] output base
+
+// Dynamic shared memory of k_sp2_step before its dense row accumulator:
+// column bitmap, touched-column list, keep flags, scan and misc words.
+__host__ __device__ inline size_t sp2_base_smem(int nb)
+{
+    const size_t nw = ((size_t)nb + 31) / 32;
+    return ((nw + 2 * (size_t)nb + kSp2ScanInts + kSp2MiscInts) * 4 + 15) & ~(size_t)15;
+}
 
 __device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total)
 {
-    // exclusive scan over 256 threads; sh holds >= 8 ints
+    // exclusive scan over the kSp2Threads threads; sh holds one int per warp
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int x = v;
     for (int o = 1; o < 32; o <<= 1) {
@@ -167,11 +178,9 @@ __global__ void __launch_bounds__(kSp2Threads)
     uint32_t *bm = reinterpret_cast<uint32_t *>(smraw);       // nw words
     int32_t *list = reinterpret_cast<int32_t *>(bm + nw);     // nb entries
     int32_t *keep = list + nb;                                // nb entries
-    int *scan = keep + nb;                                    // 8 ints
-    int *misc = scan + 8;                                     // [0]=total, [1]=kept, [2]=base
-    size_t off = (size_t)(nw + 2 * nb + 16) * 4;
-    off = (off + 15) & ~(size_t)15;
-    T *acc = acc_in_smem ? reinterpret_cast<T *>(smraw + off) : gacc + (size_t)blockIdx.x * nb * 16;
+    int *scan = keep + nb;                                    // kSp2ScanInts
+    int *misc = scan + kSp2ScanInts;                          // [0]=total, [1]=kept, [2]=base
+    T *acc = acc_in_smem ? reinterpret_cast<T *>(smraw + sp2_base_smem(nb)) : gacc + (size_t)blockIdx.x * nb * 16;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int l16 = lane & 15, half = lane >> 4, r = l16 >> 2, s = l16 & 3;
     for (int i = tid; i < nw; i += kSp2Threads) bm[i] = 0u;
@@ -433,8 +442,7 @@ int sp2_run(tb_ctx *ctx, double *diagP_h, double *q_h, double *e_band, tb_report
     int it = 0;
     double idem = INFINITY, prev1 = INFINITY, prev2 = INFINITY, trX = 0.0;
     // shared-memory budget of k_sp2_step
-    const int nw = (nb + 31) / 32;
-    size_t base_smem = ((size_t)(nw + 2 * nb + 16) * 4 + 15) & ~(size_t)15;
+    const size_t base_smem = sp2_base_smem(nb);
     size_t acc_bytes = (size_t)nb * 16 * sizeof(T);
     int dev_smem = 0;
     cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
