@@ -578,39 +578,16 @@ int build_pipe_plan(tb_ctx *ctx, const std::vector<int32_t> &brow, const std::ve
     std::vector<int32_t> hdr((size_t)G * 8, 0), rec, nptr(G + 1, 0), nbr;
     std::vector<std::vector<int32_t>> grun(G);
     int maxU = 0, maxBlk = 0, rec_cap = 0, maxRuns = 0;
+    std::vector<int32_t> U;
     for (int g = 0; g < G; g++) {
-        const int I0 = g * R, I1 = std::min(nb, I0 + R), tb0 = brow[I0];
-        std::vector<int32_t> U(bcol.begin() + tb0, bcol.begin() + brow[I1]);
-        std::sort(U.begin(), U.end());
-        U.erase(std::unique(U.begin(), U.end()), U.end());
-        const int nu = (int)U.size();
-        const size_t rstart = rec.size();
-        std::vector<int32_t> &runs = grun[g];
+        const int I0 = g * R, I1 = std::min(nb, I0 + R);
+        int32_t *h = &hdr[(size_t)g * 8];
+        pipe_group_records(brow.data(), bcol.data(), I0, I1, 0, h, rec, grun[g], U);
         for (int J : U)  // U is sorted, so the owner groups come in order
             if (nbr.size() == (size_t)nptr[g] || nbr.back() != J / R) nbr.push_back(J / R);
         nptr[g + 1] = (int32_t)nbr.size();
-        for (int I = I0; I <= I1; I++) rec.push_back(brow[I] - tb0);
-        for (int t = tb0; t < brow[I1]; t++)
-            rec.push_back((int32_t)(std::lower_bound(U.begin(), U.end(), bcol[t]) - U.begin()));
-        for (int I = I0; I < I1; I++) rec.push_back((int32_t)(std::lower_bound(U.begin(), U.end(), I) - U.begin()));
-        while ((rec.size() - rstart) % 4) rec.push_back(0);
-        for (int k = 0; k < nu;) {
-            int e = k + 1;
-            while (e < nu && U[e] == U[e - 1] + 1) e++;
-            runs.insert(runs.end(), {U[k], e - k, k, 0});
-            k = e;
-        }
-        int32_t *h = &hdr[(size_t)g * 8];
-        h[0] = nu;
-        h[1] = tb0;
-        h[2] = brow[I1] - tb0;
-        h[3] = (int32_t)rstart;
-        h[4] = (int32_t)(rec.size() - rstart);
-        h[5] = 0;
-        h[6] = (int32_t)(runs.size() / 4);
         maxRuns = std::max(maxRuns, h[6]);
-        h[7] = I1 - I0;
-        maxU = std::max(maxU, nu);
+        maxU = std::max(maxU, h[0]);
         maxBlk = std::max(maxBlk, h[2]);
         rec_cap = std::max(rec_cap, h[4]);
     }
@@ -1144,6 +1121,37 @@ void free_all(tb_ctx *ctx)
 }  // namespace
 
 namespace tb {
+
+void pipe_group_records(const int32_t *brow, const int32_t *bcol, int I0, int I1, int64_t blk0, int32_t *h,
+                        std::vector<int32_t> &rec, std::vector<int32_t> &runs, std::vector<int32_t> &U)
+{
+    const int tb0 = brow[I0];
+    U.assign(bcol + tb0, bcol + brow[I1]);
+    std::sort(U.begin(), U.end());
+    U.erase(std::unique(U.begin(), U.end()), U.end());
+    const int nu = (int)U.size();
+    const size_t rstart = rec.size();
+    for (int I = I0; I <= I1; I++) rec.push_back(brow[I] - tb0);
+    for (int t = tb0; t < brow[I1]; t++)
+        rec.push_back((int32_t)(std::lower_bound(U.begin(), U.end(), bcol[t]) - U.begin()));
+    for (int I = I0; I < I1; I++) rec.push_back((int32_t)(std::lower_bound(U.begin(), U.end(), I) - U.begin()));
+    while ((rec.size() - rstart) % 4) rec.push_back(0);
+    runs.clear();
+    for (int k = 0; k < nu;) {
+        int e = k + 1;
+        while (e < nu && U[e] == U[e - 1] + 1) e++;
+        runs.insert(runs.end(), {U[k], e - k, k, 0});
+        k = e;
+    }
+    h[0] = nu;
+    h[1] = (int32_t)(blk0 + tb0);
+    h[2] = brow[I1] - tb0;
+    h[3] = (int32_t)rstart;
+    h[4] = (int32_t)(rec.size() - rstart);
+    h[5] = I0;
+    h[6] = (int32_t)(runs.size() / 4);
+    h[7] = I1 - I0;
+}
 
 // Validation and conversion of a PETSc-style CSR (4 orbitals per atom) to
 // symmetrised 4x4 BSR on the host: the pattern of H + H^T with every diagonal

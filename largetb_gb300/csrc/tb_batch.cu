@@ -2,11 +2,15 @@
 //
 // The structures are concatenated block-diagonally: structure s owns block
 // rows [ao_s, ao_{s+1}) and orbitals [4 ao_s, 4 ao_{s+1}).  Each structure is
-// one identity slab (all of its columns, B_s = n_s rounded up to 64), so every
-// Chebyshev step of every still-active structure is ONE launch over a unit
-// list of (structure, row group, 64-column chunk); row groups never cross a
-// structure boundary and stage their referenced rows of T_k through shared
-// memory as the single-structure staged kernel does.  After each step a
+// one identity slab (all of its columns, B_s = n_s rounded up to 64, stored
+// chunk-major [B_s/64][n_s][64]), so every Chebyshev step of every
+// still-active structure is ONE launch over a list of (structure, row group,
+// 64-column chunk) tiles; row groups never cross a structure boundary.  The
+// step is the pipelined kernel (k_cheb_f32_pipe over a tile list: one
+// persistent CTA per SM, bulk copies of each tile's halo rows into a
+// shared-memory ring); when its stage does not fit, or fp32_kernel asks for
+// TB_FP32_STAGED, k_bt_cheb_f32 stages each unit through shared memory as the
+// single-structure staged kernel does.  After each step a
 // reduction turns the per-group column dot products into moments, so the
 // scratch holds one step of partials.  Gershgorin scaling, the damped DOS,
 // the mu multisection, the Fermi coefficients, charges, band energy and the
@@ -167,14 +171,14 @@ __global__ void k_bt_identity(const Unit *__restrict__ units, int nunits, const 
     const int u = blockIdx.x;
     if (u >= nunits) return;
     const Unit un = units[u];
-    const int ao = s_ao[un.s], B = s_B[un.s];
+    const int ao = s_ao[un.s], ns = 4 * (s_ao[un.s + 1] - ao);
     const int I0 = grp_I0[un.g], I1 = grp_I0[un.g + 1];
-    float *T = T0 + s_toff[un.s];
+    float *T = T0 + s_toff[un.s] + (int64_t)un.chunk * ns * kBtCols;  // chunk-major [B/64][n_s][64]
     const int col0 = un.chunk * kBtCols;
     for (int e = threadIdx.x; e < (I1 - I0) * 4 * kBtCols; e += blockDim.x) {
         const int rr = e / kBtCols, j = e % kBtCols;
         const int row = 4 * (I0 - ao) + rr;
-        T[(int64_t)row * B + col0 + j] = (row == col0 + j) ? 1.f : 0.f;
+        T[(int64_t)row * kBtCols + j] = (row == col0 + j) ? 1.f : 0.f;
     }
 }
 
@@ -199,9 +203,11 @@ __global__ void __launch_bounds__(32 * kBtWarps)
     int *sR = sL + maxBlk;
     const Unit un = units[blockIdx.x];
     const int s = un.s, g = un.g, tid = threadIdx.x;
-    const int ao = s_ao[s], B = s_B[s];
-    const float *Tin = Tin_base + s_toff[s];
-    float *Tout = Tout_base + s_toff[s];
+    const int ao = s_ao[s], B = s_B[s], ns = 4 * (s_ao[s + 1] - ao);
+    // this unit's 64-column chunk of the structure's chunk-major slabs
+    const int64_t coff = s_toff[s] + (int64_t)un.chunk * ns * kBtCols;
+    const float *Tin = Tin_base + coff;
+    float *Tout = Tout_base + coff;
     const int I0 = grp_I0[g], I1 = grp_I0[g + 1], nr = I1 - I0;
     const int u0 = grp_ptr[g], nu = grp_ptr[g + 1] - u0;
     const int tb0 = rowptr[I0], nbk = rowptr[I1] - tb0;
@@ -214,12 +220,12 @@ __global__ void __launch_bounds__(32 * kBtWarps)
         for (int idx = tid; idx < nr * 64; idx += blockDim.x) {
             const int r = idx >> 6, m = (idx >> 4) & 3, sg = idx & 15;
             cpa16(sP + (r * 4 + m) * kBtCols + sg * 4,
-                  Tout + (int64_t)(4 * (I0 - ao + r) + m) * B + col0 + sg * 4);
+                  Tout + (int64_t)(4 * (I0 - ao + r) + m) * kBtCols + sg * 4);
         }
     __syncthreads();
     for (int idx = tid; idx < nu * 64; idx += blockDim.x) {
         const int u = idx >> 6, m = (idx >> 4) & 3, sg = idx & 15;
-        cpa16(sT + (u * 4 + m) * kBtCols + sg * 4, Tin + (int64_t)(4 * sU[u] + m) * B + col0 + sg * 4);
+        cpa16(sT + (u * 4 + m) * kBtCols + sg * 4, Tin + (int64_t)(4 * sU[u] + m) * kBtCols + sg * 4);
     }
     cpa_wait();
     __syncthreads();
@@ -245,7 +251,7 @@ __global__ void __launch_bounds__(32 * kBtWarps)
             const float2 ov = *reinterpret_cast<const float2 *>(own + q * kBtCols);
             float2 o = acc[q];
             if (!first) o = cheb_next2(acc[q], *reinterpret_cast<const float2 *>(sP + (r * 4 + q) * kBtCols + c));
-            *reinterpret_cast<float2 *>(Tout + (int64_t)(4 * (I - ao) + q) * B + col0 + c) = o;
+            *reinterpret_cast<float2 *>(Tout + (int64_t)(4 * (I - ao) + q) * kBtCols + c) = o;
             ee = __ffma2_rn(ov, ov, ee);
             eo = __ffma2_rn(ov, o, eo);
         }
@@ -698,8 +704,14 @@ struct tb_batch {
     float *x32 = nullptr, *xdiag32 = nullptr, *T0 = nullptr, *T1 = nullptr;
     Unit *units = nullptr;
     int units_cap = 0;
+    // pipelined step (k_cheb_f32_pipe over a tile list): its plan (stages ==
+    // 0: unavailable, the staged step k_bt_cheb_f32 runs) and tile list
+    PipePlan pl;
+    PipeBatchTile *ptiles = nullptr;
+    int ptiles_cap = 0;
     DevState *st = nullptr;
     std::vector<int32_t> h_ao, h_B, h_g0, h_grpI0;
+    std::vector<int64_t> h_toff, h_poff;
     // the SCC iteration as a CUDA graph, captured per active set (its grid
     // sizes and unit list change only when a structure converges)
     cudaGraphExec_t graph = nullptr;
@@ -740,6 +752,63 @@ void bfree(tb_batch *b)
     for (void *p : b->allocs) cudaFree(p);
     b->allocs.clear();
     b->built = false;
+}
+
+// Plan of the pipelined step over the batch's row groups (the groups of
+// k_bt_cheb_f32: kBtR block rows inside each structure, numbered across the
+// batch); rowptr: the concatenated block-row pointers.  Leaves b->pl.stages
+// at 0 when a stage does not fit in shared memory.
+int batch_pipe_plan(tb_batch *b, const std::vector<int32_t> &rowptr)
+{
+    b->pl = PipePlan{};
+    std::vector<int32_t> hdr, rec, U, runs;
+    std::vector<std::vector<int32_t>> grun;
+    int maxU = 0, maxBlk = 0, rec_cap = 0, maxRuns = 0;
+    for (int s = 0; s < b->S; s++) {
+        const HostBsr &hb = b->hb[s];
+        const int nb = b->natoms[s];
+        for (int I0 = 0; I0 < nb; I0 += kBtR) {
+            hdr.resize(hdr.size() + 8);
+            pipe_group_records(hb.brow.data(), hb.bcol.data(), I0, std::min(nb, I0 + kBtR), rowptr[b->h_ao[s]],
+                               &hdr[hdr.size() - 8], rec, runs, U);
+            grun.push_back(runs);
+            const int32_t *h = &hdr[hdr.size() - 8];
+            maxU = std::max(maxU, h[0]);
+            maxBlk = std::max(maxBlk, h[2]);
+            rec_cap = std::max(rec_cap, h[4]);
+            maxRuns = std::max(maxRuns, h[6]);
+        }
+    }
+    const size_t stage_bytes = cheb_f32_pipe_stage_bytes(kBtR, maxU, maxBlk, rec_cap);
+    int stages = 3;
+    while (stages >= 2 && cheb_f32_pipe_smem(stage_bytes, stages) > 227 * 1024) stages--;
+    int per_sm = 0;
+    if (stages < 2 || cheb_f32_pipe_configure(cheb_f32_pipe_smem(stage_bytes, stages), &per_sm, true) != 0 ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return TB_OK;  // the staged step stays
+    }
+    const int G = (int)grun.size();
+    const int run_stride = (maxRuns + 31) / 32 * 32;
+    std::vector<int32_t> runs_all((size_t)G * run_stride * 4, 0);
+    for (int g = 0; g < G; g++)
+        std::copy(grun[g].begin(), grun[g].end(), runs_all.begin() + (size_t)g * run_stride * 4);
+    int rc;
+    if ((rc = bupload(b, b->pl.hdr, hdr)) || (rc = bupload(b, b->pl.runs, runs_all)) ||
+        (rc = bupload(b, b->pl.rec, rec)) || (rc = balloc(b, b->pl.err, 1)))
+        return rc;
+    cudaMemsetAsync(b->pl.err, 0, sizeof(int32_t), b->stream);
+    int nsm = 152;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->p.device);
+    b->pl.R = kBtR;
+    b->pl.G = G;
+    b->pl.maxU = maxU;
+    b->pl.maxBlk = maxBlk;
+    b->pl.stages = stages;
+    b->pl.stage_bytes = stage_bytes;
+    b->pl.nsm = nsm * per_sm;
+    b->pl.run_stride = run_stride;
+    return TB_OK;
 }
 
 // Concatenate the structures and lay out groups, slabs and scratch.
@@ -827,6 +896,8 @@ int batch_build(tb_batch *b)
     b->p_doubles = poff;
     b->h_ao = s_ao;
     b->h_B = s_B;
+    b->h_toff = s_toff;
+    b->h_poff = s_poff;
     b->h_g0 = s_g0;
     b->h_grpI0 = grp_I0;
     int nq_cap = 1 << 14;
@@ -899,6 +970,7 @@ int batch_build(tb_batch *b)
     cudaError_t e = cudaFuncSetAttribute(k_bt_cheb_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          smem_optin_max((const void *)k_bt_cheb_f32));
     if (e != cudaSuccess) return bfail(b, TB_ERR_CUDA, cudaGetErrorString(e));
+    BT(batch_pipe_plan(b, rowptr));
     e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) return bfail(b, TB_ERR_CUDA, cudaGetErrorString(e));
 #undef BT
@@ -953,6 +1025,7 @@ int tb_batch_destroy(tb_batch *b)
     bfree(b);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->units) cudaFree(b->units);
+    if (b->ptiles) cudaFree(b->ptiles);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return TB_OK;
@@ -1016,6 +1089,9 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
     const size_t smem = bt_smem(b->maxU, b->maxBlk);
     int it = 0, rc = TB_OK;
     std::vector<Unit> units;
+    std::vector<PipeBatchTile> ptiles;
+    // the pipelined step unless its plan does not fit or fp32_kernel asks for the staged one
+    const bool pipe = b->pl.stages > 0 && b->p.fp32_kernel != TB_FP32_STAGED;
     std::vector<DevState> hs(S);
     for (it = 1; it <= b->p.scc_max_iter; it++) {
         units.clear();
@@ -1027,6 +1103,34 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
                 for (int ch = 0; ch < chunks; ch++) units.push_back(Unit{s, gg, ch, 0});
             act_cols += 4 * (b->h_ao[s + 1] - b->h_ao[s]);
         }
+        // the pipelined step's tiles: by structure, chunk, then group (the
+        // groups that share halo rows run close together)
+        ptiles.clear();
+        for (int s = 0; pipe && s < S; s++) {
+            if (!act[s]) continue;
+            const int64_t ns = 4 * (int64_t)(b->h_ao[s + 1] - b->h_ao[s]);
+            for (int ch = 0; ch < b->h_B[s] / kBtCols; ch++)
+                for (int gg = b->h_g0[s]; gg < b->h_g0[s + 1]; gg++)
+                    ptiles.push_back(PipeBatchTile{b->h_toff[s] + ch * ns * kBtCols,
+                                                   b->h_poff[s] + ((int64_t)(gg - b->h_g0[s]) * b->h_B[s] +
+                                                                   ch * kBtCols) * 2,
+                                                   gg, {0, 0, 0}});
+        }
+        if ((int)ptiles.size() > b->ptiles_cap) {
+            if (b->graph) {  // holds the old tile-list pointer
+                cudaGraphExecDestroy(b->graph);
+                b->graph = nullptr;
+            }
+            if (b->ptiles) cudaFree(b->ptiles);
+            b->ptiles_cap = (int)ptiles.size();
+            if (cudaMalloc(&b->ptiles, sizeof(PipeBatchTile) * b->ptiles_cap) != cudaSuccess) {
+                b->ptiles = nullptr;
+                b->ptiles_cap = 0;
+                rc = bfail(b, TB_ERR_OUT_OF_MEMORY, "cudaMalloc(tiles)");
+                break;
+            }
+        }
+        const int npt = (int)ptiles.size();
         if ((int)units.size() > b->units_cap) {
             if (b->graph) {  // holds the old unit-list pointer
                 cudaGraphExecDestroy(b->graph);
@@ -1047,8 +1151,11 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
         // converges) and replayed after that, or issued directly (no_graphs).
         const bool use_graph = !b->p.no_graphs;
         const bool fresh = !b->graph || b->graph_act != act;
-        if (fresh || !use_graph)
+        if (fresh || !use_graph) {
             cudaMemcpyAsync(b->units, units.data(), sizeof(Unit) * units.size(), cudaMemcpyHostToDevice, st);
+            if (npt)
+                cudaMemcpyAsync(b->ptiles, ptiles.data(), sizeof(PipeBatchTile) * npt, cudaMemcpyHostToDevice, st);
+        }
         const bool capture = use_graph && fresh;
         auto record = [&](cudaEvent_t e) {
             if (capture)
@@ -1067,11 +1174,14 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
                 const bool odd = (k + 1) & 1;
                 const float *Tin = odd ? b->T0 : b->T1;
                 float *Tout = odd ? b->T1 : b->T0;
-                k_bt_cheb_f32<<<nu, 32 * kBtWarps, smem, st>>>(b->units, b->s_ao, b->s_B, b->s_toff, b->s_poff,
-                                                                b->s_g0, b->grp_I0, b->rowptr, b->lcol, b->lself,
-                                                                b->grp_ptr, b->grp_rows, b->x32, Tin, Tout, k == 0,
-                                                                reinterpret_cast<float2 *>(b->partial), b->maxU,
-                                                                b->maxBlk);
+                if (pipe)
+                    launch_cheb_f32_pipe_batch(st, b->pl, b->ptiles, npt, b->x32, b->T0, b->T1, k,
+                                               reinterpret_cast<float2 *>(b->partial));
+                else
+                    k_bt_cheb_f32<<<nu, 32 * kBtWarps, smem, st>>>(
+                        b->units, b->s_ao, b->s_B, b->s_toff, b->s_poff, b->s_g0, b->grp_I0, b->rowptr, b->lcol,
+                        b->lself, b->grp_ptr, b->grp_rows, b->x32, Tin, Tout, k == 0,
+                        reinterpret_cast<float2 *>(b->partial), b->maxU, b->maxBlk);
                 k_bt_finalize<<<(n + 255) / 256, 256, 0, st>>>(n, k, M, b->s_of_atom, b->active, b->s_ao, b->s_B,
                                                                b->s_poff, b->s_g0,
                                                                reinterpret_cast<const float2 *>(b->partial),
@@ -1161,6 +1271,14 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
     cudaEventDestroy(e1);
     cudaEventDestroy(m0);
     cudaEventDestroy(m1);
+    if (rc == TB_OK && pipe) {  // bounded waits of the pipelined step that gave up
+        int32_t perr = 0;
+        cudaMemcpy(&perr, b->pl.err, sizeof(int32_t), cudaMemcpyDeviceToHost);
+        if (perr) {
+            cudaMemset(b->pl.err, 0, sizeof(int32_t));
+            rc = bfail(b, TB_ERR_CUDA, "pipelined batch step: a bounded wait timed out");
+        }
+    }
     if (rc == TB_OK) {
         for (int s = 0; s < S; s++) {
             if (hs[s].status) {

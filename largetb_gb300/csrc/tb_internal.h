@@ -80,6 +80,15 @@ struct PipePlan {
     int32_t *err = nullptr;  // device error flag (bounded waits)
 };
 
+// One tile of the batched pipelined step: a row group of one structure x one
+// 64-column chunk of that structure's chunk-major slabs.
+struct PipeBatchTile {
+    int64_t coff;   // float offset of the chunk in the slab buffers ([B_s/64][n_s][64] per structure)
+    int64_t pbase;  // float2 offset of the tile's column sums (hi, lo) in the partial array
+    int32_t g;      // row group: index into the plan's headers and copy runs
+    int32_t pad[3];
+};
+
 // Chebyshev step kernels of the FP32 form (values of tb_params.fp32_kernel).
 enum StepKind {
     kKindAuto = 0,
@@ -232,7 +241,8 @@ size_t cheb_f32_pipe_stage_bytes(int R, int maxU, int maxBlk, int rec_cap);
 // identity columns in the chunk-major slab layout [B/64][n][64] of the pipelined kernel
 void launch_slab_identity_cm(cudaStream_t st, float *T0, int n, int B, int c0);
 size_t cheb_f32_pipe_smem(size_t stage_bytes, int stages);
-int cheb_f32_pipe_configure(size_t smem, int *ctas_per_sm);  // returns a cudaError_t
+// batch: the instance of launch_cheb_f32_pipe_batch.  Returns a cudaError_t.
+int cheb_f32_pipe_configure(size_t smem, int *ctas_per_sm, bool batch = false);
 // Steps k0 .. k0+steps-1 of a slab held in T0/T1 (chunk-major; step k reads
 // T_k from T0 when k is even); partial: float2 (hi, lo) pairs in the slots of
 // the double partial array, block k - k0 per step.  multi: one cooperative
@@ -240,6 +250,10 @@ int cheb_f32_pipe_configure(size_t smem, int *ctas_per_sm);  // returns a cudaEr
 // Returns a cudaError_t.
 int launch_cheb_f32_pipe(cudaStream_t st, const DevMatrix &m, const PipePlan &pl, float *T0, float *T1, int B,
                          int k0, int steps, float2 *partial, bool multi);
+// Step k of every tile of a batch of structures (one plain launch): tiles
+// ordered by structure, chunk and group; x32: the concatenated FP32 blocks.
+void launch_cheb_f32_pipe_batch(cudaStream_t st, const PipePlan &pl, const PipeBatchTile *tiles, int ntiles,
+                                const float *x32, float *T0, float *T1, int k, float2 *partial);
 void launch_f32_finalize_pairs(cudaStream_t st, const DevMatrix &m, const float2 *partial, int K, int rowgroups,
                                int B, int c0, double *d, int M);
 int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const StagePlan &sp,
@@ -247,6 +261,17 @@ int launch_cheb_step_f32_staged(cudaStream_t st, const DevMatrix &m, const Stage
                                 float2 *partial_k);
 void launch_moment_sums(cudaStream_t st, const double *d, int n, int nmom, double *mom);
 void launch_cos_table(cudaStream_t st, int nq_cap, double *tab);
+
+// Records of the pipelined step kernel for the row group [I0, I1) of a block
+// pattern (brow / bcol over one structure, rows local to it): the 8-int header
+// at h (distinct referenced block rows nu, first block blk0 + brow[I0], blocks,
+// record offset, record length, I0, copy runs, rows), the index record
+// appended to rec (row pointers, slot of each block's column among the
+// distinct rows, slot of each own row; padded to a multiple of 4) and the copy
+// runs of consecutive rows (first row, rows, first slot, 0).  U returns the
+// sorted distinct referenced rows.
+void pipe_group_records(const int32_t *brow, const int32_t *bcol, int I0, int I1, int64_t blk0, int32_t *h,
+                        std::vector<int32_t> &rec, std::vector<int32_t> &runs, std::vector<int32_t> &U);
 void launch_dos_nodes(cudaStream_t st, const double *g, const double *mom, int M,
                       const DevState *state, int nq_cap, const double *tab, double *rho);
 void launch_bisect_round(cudaStream_t st, const double *rho, const double *g, const double *mom,

@@ -84,6 +84,8 @@ struct PipeArgs {
     float2 *partial;   // [steps][G][B][2] pairs; step k writes block k - k0
     int32_t *flags;    // [G * nchunk] completed steps per tile (multi-step launch), or null
     int32_t *err;
+    const PipeBatchTile *tiles;  // batched form: the tile list (slab and partial offsets per tile)
+    int ntiles;
 };
 
 __device__ __forceinline__ uint32_t sm_addr(const void *p)
@@ -207,6 +209,10 @@ __device__ __forceinline__ bool wait_neighbours(const PipeArgs &a, int chunk, in
     return true;
 }
 
+// kBatch: tiles come from a.tiles (row groups of many structures, each
+// structure its own chunk-major slabs and partial block); else tile t is
+// (chunk t / G, group t % G) of one slab.
+template <bool kBatch>
 __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -234,7 +240,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
-    const int ntiles = a.G * a.nchunk;
+    const int ntiles = kBatch ? a.ntiles : a.G * a.nchunk;
     const int mine = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const int total = mine * a.steps;  // this CTA's tiles over all steps, step-major
     const int oT = 0, oP = a.maxU * 4 * kPipeCols, oX = oP + a.R * 4 * kPipeCols,
@@ -268,25 +274,39 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         // ---------------- producer ----------------
         int i = 0;
         int4 ha = make_int4(0, 0, 0, 0), hb = ha, run = ha;
+        int gnext = 0;          // group of the next tile
+        int64_t cnext = 0;      // batched form: its chunk offset
         if (total > 0) {
-            const int g = (int)blockIdx.x % a.G;
-            ha = __ldg(a.hdr + 2 * g);
-            hb = __ldg(a.hdr + 2 * g + 1);
-            run = __ldg(a.runs + (int64_t)g * a.run_stride + lane);
+            if constexpr (kBatch) {
+                gnext = a.tiles[blockIdx.x].g;
+                cnext = a.tiles[blockIdx.x].coff;
+            } else {
+                gnext = (int)blockIdx.x % a.G;
+            }
+            ha = __ldg(a.hdr + 2 * gnext);
+            hb = __ldg(a.hdr + 2 * gnext + 1);
+            run = __ldg(a.runs + (int64_t)gnext * a.run_stride + lane);
         }
         for (; i < total; ++i) {
             const int k = a.k0 + i / mine;
             const int t = (int)blockIdx.x + (i % mine) * (int)gridDim.x;
-            const int chunk = t / a.G, g = t - chunk * a.G;
+            const int g = gnext;
+            const int chunk = kBatch ? 0 : t / a.G;
+            const int64_t coff = kBatch ? cnext : (int64_t)chunk * chunk_floats;
             const int nu = ha.x, tb0 = ha.y, nbk = ha.z, r0 = ha.w;
-            const int rl = hb.x, nruns = hb.z, nr = hb.w;
+            const int rl = hb.x, I0 = hb.y, nruns = hb.z, nr = hb.w;
             const int4 cur = run;
             if (i + 1 < total) {  // header and runs of the next tile
                 const int tn = (int)blockIdx.x + ((i + 1) % mine) * (int)gridDim.x;
-                const int gn = tn % a.G;
-                ha = __ldg(a.hdr + 2 * gn);
-                hb = __ldg(a.hdr + 2 * gn + 1);
-                run = __ldg(a.runs + (int64_t)gn * a.run_stride + lane);
+                if constexpr (kBatch) {
+                    gnext = a.tiles[tn].g;
+                    cnext = a.tiles[tn].coff;
+                } else {
+                    gnext = tn % a.G;
+                }
+                ha = __ldg(a.hdr + 2 * gnext);
+                hb = __ldg(a.hdr + 2 * gnext + 1);
+                run = __ldg(a.runs + (int64_t)gnext * a.run_stride + lane);
             }
             // this tile's neighbour flags, read before the stage wait
             int seen = 0x7fffffff;
@@ -308,7 +328,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                 mbar_arrive_expect_tx(&full[s], (uint32_t)nu * 1024u + (k == 0 ? 0u : (uint32_t)nr * 1024u) +
                                                     (uint32_t)nbk * 64u + (uint32_t)rl * 4u);
             __syncwarp();
-            const float *srcT = Tin + (int64_t)chunk * chunk_floats;
+            const float *srcT = Tin + coff;
             if (lane < nruns)
                 bulk_g2s(stg + oT + cur.z * 4 * kPipeCols, srcT + (int64_t)cur.x * 4 * kPipeCols,
                          (uint32_t)cur.y * 1024u, &full[s]);
@@ -321,8 +341,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                 bulk_g2s(stg + oX, a.x32 + (int64_t)tb0 * 16, (uint32_t)nbk * 64u, &full[s]);
                 bulk_g2s(stg + oRec, a.rec + r0, (uint32_t)rl * 4u, &full[s]);
                 if (k > 0)
-                    bulk_g2s(stg + oP, Tprev + (int64_t)chunk * chunk_floats + (int64_t)g * a.R * 4 * kPipeCols,
-                             (uint32_t)nr * 1024u, &full[s]);
+                    bulk_g2s(stg + oP, Tprev + coff + (int64_t)I0 * 4 * kPipeCols, (uint32_t)nr * 1024u, &full[s]);
             }
         }
         if (*s_abort) {
@@ -342,9 +361,25 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         const int k = a.k0 + i / mine;
         const int t = (int)blockIdx.x + (i % mine) * (int)gridDim.x;
         const int s = i % a.stages;
-        const int chunk = t / a.G, g = t - chunk * a.G;
-        const int I0 = g * a.R, nr = min(a.nb, I0 + a.R) - I0;
-        float *out = ((k & 1) ? a.T0 : a.T1) + (int64_t)chunk * chunk_floats + (int64_t)I0 * 4 * kPipeCols + c;
+        int g, I0, nr;
+        int64_t coff, pbase;  // slab offset of the tile's chunk; float2 offset of its column sums
+        if constexpr (kBatch) {
+            const PipeBatchTile bt = a.tiles[t];
+            const int4 hb = __ldg(a.hdr + 2 * bt.g + 1);
+            g = bt.g;
+            coff = bt.coff;
+            pbase = bt.pbase;
+            I0 = hb.y;
+            nr = hb.w;
+        } else {
+            const int chunk = t / a.G;
+            g = t - chunk * a.G;
+            I0 = g * a.R;
+            nr = min(a.nb, I0 + a.R) - I0;
+            coff = (int64_t)chunk * chunk_floats;
+            pbase = (((int64_t)(k - a.k0) * a.G + g) * a.B + chunk * kPipeCols) * 2;
+        }
+        float *out = ((k & 1) ? a.T0 : a.T1) + coff + (int64_t)I0 * 4 * kPipeCols + c;
         // pairs (hi, lo), packed over columns (c, c+1): <T_k,T_k> in (eh, el),
         // <T_k,T_{k+1}> in (oh, ol)
         float2 eh = make_float2(0.f, 0.f), el = eh, oh = eh, ol = eh;
@@ -410,8 +445,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                     pair_add(hsum, lsum, v.x);
                     lsum += v.y;
                 }
-                a.partial[(((int64_t)(k - a.k0) * a.G + g) * a.B + chunk * kPipeCols + j) * 2 + which] =
-                    make_float2(hsum, lsum);
+                a.partial[pbase + j * 2 + which] = make_float2(hsum, lsum);
             }
             __syncwarp();
             if (lane == 0) {
@@ -483,14 +517,15 @@ size_t cheb_f32_pipe_smem(size_t stage_bytes, int stages)
 
 int cheb_f32_pipe_max_rows() { return kPipeCW * 3; }
 
-int cheb_f32_pipe_configure(size_t smem, int *ctas_per_sm)
+int cheb_f32_pipe_configure(size_t smem, int *ctas_per_sm, bool batch)
 {
-    const int lim = smem_optin_max((const void *)k_cheb_f32_pipe);
+    const void *fn = batch ? (const void *)k_cheb_f32_pipe<true> : (const void *)k_cheb_f32_pipe<false>;
+    const int lim = smem_optin_max(fn);
     if ((int)smem > lim) return (int)cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_cheb_f32_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (e != cudaSuccess) return (int)e;
     *ctas_per_sm = 0;
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, k_cheb_f32_pipe, kPipeThreads, smem);
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, kPipeThreads, smem);
 }
 
 void launch_f32_finalize_pairs(cudaStream_t st, const DevMatrix &m, const float2 *partial, int K, int rowgroups,
@@ -535,18 +570,49 @@ int launch_cheb_f32_pipe(cudaStream_t st, const DevMatrix &m, const PipePlan &pl
     a.partial = partial;
     a.flags = multi ? pl.flags : nullptr;
     a.err = pl.err;
+    a.tiles = nullptr;
+    a.ntiles = 0;
     const int ntiles = pl.G * a.nchunk;
     const int grid = std::min(ntiles, pl.nsm);
     const size_t smem = cheb_f32_pipe_smem(pl.stage_bytes, pl.stages);
     if (!multi) {
-        k_cheb_f32_pipe<<<grid, kPipeThreads, smem, st>>>(a);
+        k_cheb_f32_pipe<false><<<grid, kPipeThreads, smem, st>>>(a);
         return (int)cudaSuccess;
     }
     cudaError_t e = cudaMemsetAsync(pl.flags, 0, sizeof(int32_t) * (size_t)ntiles, st);
     if (e != cudaSuccess) return (int)e;
     void *args[] = {&a};
-    return (int)cudaLaunchCooperativeKernel((const void *)k_cheb_f32_pipe, dim3(grid), dim3(kPipeThreads), args,
+    return (int)cudaLaunchCooperativeKernel((const void *)k_cheb_f32_pipe<false>, dim3(grid), dim3(kPipeThreads), args,
                                             smem, st);
+}
+
+void launch_cheb_f32_pipe_batch(cudaStream_t st, const PipePlan &pl, const PipeBatchTile *tiles, int ntiles,
+                                const float *x32, float *T0, float *T1, int k, float2 *partial)
+{
+    PipeArgs a{};
+    a.R = pl.R;
+    a.G = pl.G;
+    a.stages = pl.stages;
+    a.stage_bytes = (int)pl.stage_bytes;
+    a.maxU = pl.maxU;
+    a.maxBlk = pl.maxBlk;
+    a.run_stride = pl.run_stride;
+    a.k0 = k;
+    a.steps = 1;
+    a.hdr = reinterpret_cast<const int4 *>(pl.hdr);
+    a.runs = reinterpret_cast<const int4 *>(pl.runs);
+    a.rec = pl.rec;
+    a.x32 = x32;
+    a.T0 = T0;
+    a.T1 = T1;
+    a.partial = partial;
+    a.flags = nullptr;
+    a.err = pl.err;
+    a.tiles = tiles;
+    a.ntiles = ntiles;
+    const int grid = std::min(ntiles, pl.nsm);
+    if (grid < 1) return;
+    k_cheb_f32_pipe<true><<<grid, kPipeThreads, cheb_f32_pipe_smem(pl.stage_bytes, pl.stages), st>>>(a);
 }
 
 }  // namespace tb

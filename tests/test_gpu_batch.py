@@ -72,3 +72,20 @@ def test_batch_graph_replay_equals_direct_launches(gpu):
         for qa, qc in zip(a["q"], c["q"]):
             np.testing.assert_array_equal(qa, qc)
         assert a["report"]["kernel_launches"] == c["report"]["kernel_launches"]
+
+
+def test_batch_pipelined_equals_staged_step(gpu):
+    """The batch's pipelined step (persistent CTAs over a tile list of every
+    structure's row groups and chunks, bulk copies into a shared-memory ring)
+    and its staged step (one CTA per unit) run the same FP32 multiply-add
+    chain per block row; only the order in which warps' column sums are added
+    differs, so the charges agree far below the FP32 tolerance."""
+    models = [gpu.model_cristobalite(*c, sigma_ang=s, seed=sd) for c, s, sd in CASES]
+    out = {}
+    for kern in (gpu.FP32_STAGED, gpu.FP32_AUTO):
+        with gpu.Batch(models, M=120, fp32_kernel=kern) as b:
+            out[kern] = b.scc_solve()
+    a, c = out[gpu.FP32_STAGED], out[gpu.FP32_AUTO]
+    np.testing.assert_array_equal(np.asarray(a["iters"]), np.asarray(c["iters"]))
+    for qa, qc in zip(a["q"], c["q"]):
+        assert np.abs(qa - qc).max() < 1e-10
