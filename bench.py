@@ -214,14 +214,17 @@ def run_batch_bench(args, T, dev, rank):
     b = T.Batch(models, M=M, device=dev)
     for _ in range(args.warmup):
         b.scc_solve()
-    ts, am = [], []
+    ts, am, gbs = [], [], []
     for _ in range(args.steps):
         l2_flush(dev)
         r = b.scc_solve()
         t = r["report"]["t_total_ms"] / 1e3
         ts.append(t)
         am.append(float((atoms * M * r["iters"]).sum()) / t)
+        # algorithmic bytes of the Chebyshev steps over the event-timed moment phase
+        gbs.append(r["report"]["spmm_bytes"] / (r["report"]["t_moments_ms"] / 1e3) / 1e9)
     b.close()
+    peak, src = peaks()
     # the single-structure forms looped over structures
     def loop(prec, idx):
         tot_t, tot_am = 0.0, 0.0
@@ -245,6 +248,9 @@ def run_batch_bench(args, T, dev, rank):
             "s_per_batch_solve": statistics.mean(ts), "structures": len(models),
             "atoms_total": int(atoms.sum()), "atoms_min": int(atoms.min()), "atoms_max": int(atoms.max()),
             "scc_iterations": [int(x) for x in r["iters"]],
+            "step_kernel": {"name": "k_cheb_f32_pipe<batch>", "GBps_algorithmic": statistics.mean(gbs),
+                            "frac": statistics.mean(gbs) / peak, "peak_GBps": peak, "peak_source": src,
+                            "timed": "moment phase (steps and per-step finalize), CUDA events"},
             "loop_fp32_single": {"value": loop32, "s_total": t32},
             "loop_plain_fp64_single": {"value": loop64, "structures": sub, "s_total_subset": t64},
             "speedup_vs_loop_plain_fp64": statistics.mean(am) / loop64,
