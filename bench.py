@@ -360,10 +360,12 @@ def run_all_kernels(T, dev):
         c.set_geometry(m.xyz, m.species, learned.cell_box((3, 3, 3)), rcut_bohr=4.0, gamma_diag=1.0)
         c.density()
     calls.append("set_geometry + density")
-    with T.Batch([T.model_cristobalite(*d, sigma_ang=0.05, seed=i)
-                  for i, d in enumerate([(1, 1, 2), (2, 1, 2), (2, 2, 2)])], M=60, device=dev) as b:
-        b.scc_solve()
-    calls.append("batch of 3")
+    for kern in (T.FP32_AUTO, T.FP32_STAGED):
+        with T.Batch([T.model_cristobalite(*d, sigma_ang=0.05, seed=i)
+                      for i, d in enumerate([(1, 1, 2), (2, 1, 2), (2, 2, 2)])], M=60, device=dev,
+                     fp32_kernel=kern) as b:
+            b.scc_solve()
+        calls.append(f"batch of 3, fp32 kernel {kern}")
     X = T.mlp_features(m.xyz, m.species, learned.cell_box((3, 3, 3)))
     mlp = T.MLP(device=dev, seed=2)
     mlp.train(X, np.zeros(len(X), np.float32), epochs=1, batch=256, lr=1e-3)
