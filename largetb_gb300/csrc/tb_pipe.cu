@@ -18,18 +18,24 @@
 // copy runs of the next tile are loaded while the producer waits for a free
 // stage, so no global load latency sits on its path.
 //
-// Two launch modes share the kernel:
+// Three launch modes share the kernel:
 //  - one launch per step (steps = 1);
 //  - one cooperative launch per slab running all K steps.  A tile publishes
 //    its step count in flags[tile] (release, after an mbarrier that every
-//    consumer warp arrives on after its stores); before the producer copies tile (chunk, g) of step k >= 1 it
-//    waits (acquire) until every group g' whose rows g references, g itself
-//    included, has published step k in the same chunk.  That covers both the
-//    T_k rows it reads and the T_{k-1} rows it overwrites: the block pattern is
-//    symmetric, so the groups that read rows of g at step k-1 are exactly those
-//    neighbours.  Each CTA runs its tiles in step order and all CTAs are
-//    co-resident, so the oldest unfinished step can always proceed.  The
-//    pipeline never drains between steps.
+//    consumer warp arrives on after its stores); before the producer copies
+//    tile (chunk, g) of step k >= 1 it waits (acquire) until every group g'
+//    whose rows g references, g itself included, has published step k in the
+//    same chunk.  That covers both the T_k rows it reads and the T_{k-1} rows
+//    it overwrites: the block pattern is symmetric, so the groups that read
+//    rows of g at step k-1 are exactly those neighbours.  Each CTA runs its
+//    tiles in step order and all CTAs are co-resident, so the oldest
+//    unfinished step can always proceed.  The pipeline never drains between
+//    steps;
+//  - the batched form (k_cheb_f32_pipe<true>, one launch per step): tiles
+//    come from a list over many structures, each tile naming its row group
+//    and carrying the offset of its chunk in that structure's slabs and of
+//    its column sums; a group's header holds its first (structure-local)
+//    block row.
 //
 // Column dot products <T_k,T_k> and <T_k,T_{k+1}> accumulate in FP32 over one
 // block row and then as unevaluated FP32 pairs (hi, lo) across rows and warps:
