@@ -89,3 +89,43 @@ def test_batch_pipelined_equals_staged_step(gpu):
     np.testing.assert_array_equal(np.asarray(a["iters"]), np.asarray(c["iters"]))
     for qa, qc in zip(a["q"], c["q"]):
         assert np.abs(qa - qc).max() < 1e-10
+
+
+def _plus_u(m):
+    """The reference's quartz Gamma has -U on the diagonal, under which the
+    SCC runs away; the batch tests use +U."""
+    g = m.g_vals.copy()
+    for a in range(m.natoms):
+        for k in range(m.g_rowptr[a], m.g_rowptr[a + 1]):
+            if m.g_colidx[k] == a:
+                g[k] = -g[k]
+    m.g_vals = g
+    return m
+
+
+def test_batch_ragged_structures(gpu):
+    """Structures whose atom counts are not multiples of the 24-row groups
+    (9, 18 and 81-atom alpha-quartz slabs beside a 24-atom cristobalite
+    cell): partial last groups and partial last chunks in one tile list.
+    The batch must land where the single-structure FP32 path lands; against
+    the FP64 oracle the quartz slabs show the FP32 recurrence's charge noise
+    (~1e-6 e: their surface states put levels near mu), so the oracle check
+    allows 2e-6 e and no iteration match.  Anderson history 4 (16 stored
+    residuals in 9 or 18 dimensions make the least-squares step
+    ill-conditioned)."""
+    dims = [(1, 1, 1), (2, 1, 1), (3, 3, 1)]
+    models = [_plus_u(gpu.model_quartz(*d)) for d in dims]
+    models.append(gpu.model_cristobalite(1, 1, 1, sigma_ang=0.05, seed=3))
+    oracles = [O.quartz(*d, gamma_diag=1.0) for d in dims] + [O.cristobalite(1, 1, 1, sigma_ang=0.05, seed=3)]
+    M = 120
+    with gpu.Batch(models, M=M, mix_history=4) as b:
+        r = b.scc_solve()
+    for i, (m, o) in enumerate(zip(models, oracles)):
+        with gpu.Context(M=M, precision=gpu.PREC_FP32, mix_history=4) as c:
+            c.set_model(m)
+            s = c.scc_solve()
+        assert int(r["iters"][i]) == s["iters"], (i, r["iters"][i], s["iters"])
+        assert np.abs(r["q"][i] - s["q"]).max() < 1e-7, i
+        ref = O.scc(o, O.kpe_params(M=M, kT=0.01, n_elec=o.n_elec), tol=1e-6, max_iter=100, beta=0.2, history=4)
+        assert ref["status"] == 0
+        assert np.abs(r["q"][i] - ref["q"]).max() < 2e-6, i
