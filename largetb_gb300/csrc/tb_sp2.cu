@@ -16,7 +16,8 @@
 // memory when nb * 16 values fit, else a per-CTA global slice) with a bitmap
 // of touched columns; 16 lanes compute one 4x4 product (lane = one output
 // element, 4 FMAs).  Phase B scans the bitmap in column order, forms the new
-// block, drops small blocks, and appends the compacted row to the output.
+// block (the old X_IJ located through a bitmap of row I's columns and prefix
+// counts), drops small blocks, and appends the compacted row to the output.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,11 +47,12 @@ constexpr int kSp2ScanInts = 32;  // one int per warp for block_excl_scan
 constexpr int kSp2MiscInts = 8;   // [0] total, [1] overflow, [2] output base
 
 // Dynamic shared memory of k_sp2_step before its dense row accumulator:
-// column bitmap, touched-column list, keep flags, scan and misc words.
+// bitmap of the product's columns, bitmap of row I's own columns and its
+// per-word prefix counts, touched-column list, keep flags, scan and misc words.
 __host__ __device__ inline size_t sp2_base_smem(int nb)
 {
     const size_t nw = ((size_t)nb + 31) / 32;
-    return ((nw + 2 * (size_t)nb + kSp2ScanInts + kSp2MiscInts) * 4 + 15) & ~(size_t)15;
+    return ((3 * nw + 2 * (size_t)nb + kSp2ScanInts + kSp2MiscInts) * 4 + 15) & ~(size_t)15;
 }
 
 __device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total)
@@ -176,20 +178,28 @@ __global__ void __launch_bounds__(kSp2Threads)
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nw = (nb + 31) >> 5;
     uint32_t *bm = reinterpret_cast<uint32_t *>(smraw);       // nw words
-    int32_t *list = reinterpret_cast<int32_t *>(bm + nw);     // nb entries
+    uint32_t *bmI = bm + nw;                                  // nw words: columns of row I of X
+    int32_t *prefI = reinterpret_cast<int32_t *>(bmI + nw);   // nw: row-I columns in earlier words
+    int32_t *list = prefI + nw;                               // nb entries
     int32_t *keep = list + nb;                                // nb entries
     int *scan = keep + nb;                                    // kSp2ScanInts
     int *misc = scan + kSp2ScanInts;                          // [0]=total, [1]=kept, [2]=base
     T *acc = acc_in_smem ? reinterpret_cast<T *>(smraw + sp2_base_smem(nb)) : gacc + (size_t)blockIdx.x * nb * 16;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int l16 = lane & 15, half = lane >> 4, r = l16 >> 2, s = l16 & 3;
-    for (int i = tid; i < nw; i += kSp2Threads) bm[i] = 0u;
+    for (int i = tid; i < nw; i += kSp2Threads) bm[i] = bmI[i] = 0u;
     for (size_t i = tid; i < (size_t)nb * 16; i += kSp2Threads) acc[i] = T(0);
     __syncthreads();
     double trX2 = 0.0, idem2 = 0.0, trNew = 0.0;
     float ih = 0.f, il = 0.f;  // FP32 blocks: sum of (X^2 - X)^2 as a TwoSum pair
     for (int I = blockIdx.x; I < nb; I += gridDim.x) {
         const int ri = rs[I], li = rl[I];
+        // row I's own columns as a bitmap: with per-word prefix counts it gives
+        // the position of X_IJ in the (sorted) row without a search
+        for (int t = tid; t < li; t += kSp2Threads) {
+            const int J = col[ri + t];
+            atomicOr(bmI + (J >> 5), 1u << (J & 31));
+        }
         // ---- phase A: row I of X^2 ----
         // a half warp forms one 4x4 block product: lane (r, s) loads element
         // (r, s) of B (one coalesced 64-byte load per block), gathers column s
@@ -241,8 +251,21 @@ __global__ void __launch_bounds__(kSp2Threads)
             const int wi = tid * wpt + q;
             if (wi < nw) cnt += __popc(bm[wi]);
         }
+        if (w == 0) {  // exclusive prefix of the row-I bitmap's word counts
+            int carry = 0;
+            for (int b0 = 0; b0 < nw; b0 += 32) {
+                const int c = b0 + lane < nw ? __popc(bmI[b0 + lane]) : 0;
+                int x = c;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (b0 + lane < nw) prefI[b0 + lane] = carry + x - c;
+                carry += __shfl_sync(0xffffffffu, x, 31);
+            }
+        }
         int total;
-        int pos = block_excl_scan(cnt, scan, &total);
+        int pos = block_excl_scan(cnt, scan, &total);  // its barriers also publish prefI
         for (int q = 0; q < wpt; q++) {
             const int wi = tid * wpt + q;
             if (wi >= nw) break;
@@ -264,7 +287,8 @@ __global__ void __launch_bounds__(kSp2Threads)
             const int J = valid ? list[i] : 0;
             T *a = acc + (size_t)J * 16;
             const T x2 = valid ? a[l16] : T(0);
-            const int xi = valid ? find_col<T>(col, ri, li, J) : -1;
+            const uint32_t wI = bmI[J >> 5], bI = 1u << (J & 31);  // J = 0 when !valid: in range
+            const int xi = valid && (wI & bI) ? ri + prefI[J >> 5] + __popc(wI & (bI - 1u)) : -1;
             const T xo = xi >= 0 ? blk[(size_t)xi * 16 + l16] : T(0);
             const T nv = branch < 0 ? x2 : T(2) * xo - x2;
             float nrm;
@@ -330,6 +354,7 @@ __global__ void __launch_bounds__(kSp2Threads)
             }
             a[l16] = T(0);
         }
+        for (int i = tid; i < nw; i += kSp2Threads) bmI[i] = 0u;  // read last in phase B2
         __syncthreads();
     }
     idem2 += (double)ih + (double)il;
