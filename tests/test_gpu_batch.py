@@ -107,12 +107,13 @@ def test_batch_ragged_structures(gpu):
     """Structures whose atom counts are not multiples of the 24-row groups
     (9, 18 and 81-atom alpha-quartz slabs beside a 24-atom cristobalite
     cell): partial last groups and partial last chunks in one tile list.
-    The batch must land where the single-structure FP32 path lands; against
-    the FP64 oracle the quartz slabs show the FP32 recurrence's charge noise
-    (~1e-6 e: their surface states put levels near mu), so the oracle check
-    allows 2e-6 e and no iteration match.  Anderson history 4 (16 stored
-    residuals in 9 or 18 dimensions make the least-squares step
-    ill-conditioned)."""
+    The batch must land where the single-structure FP32 path lands (both
+    stop at |dq| < 1e-6 e; their column sums are added in different orders,
+    which the SCC response amplifies to ~1e-7 e); against the FP64 oracle the
+    quartz slabs show the FP32 recurrence's charge noise (~1e-6 e: their
+    surface states put levels near mu), so the oracle check allows 2e-6 e and
+    no iteration match.  Anderson history 4 (16 stored residuals in 9 or 18
+    dimensions make the least-squares step ill-conditioned)."""
     dims = [(1, 1, 1), (2, 1, 1), (3, 3, 1)]
     models = [_plus_u(gpu.model_quartz(*d)) for d in dims]
     models.append(gpu.model_cristobalite(1, 1, 1, sigma_ang=0.05, seed=3))
@@ -124,8 +125,8 @@ def test_batch_ragged_structures(gpu):
         with gpu.Context(M=M, precision=gpu.PREC_FP32, mix_history=4) as c:
             c.set_model(m)
             s = c.scc_solve()
-        assert int(r["iters"][i]) == s["iters"], (i, r["iters"][i], s["iters"])
-        assert np.abs(r["q"][i] - s["q"]).max() < 1e-7, i
+        assert abs(int(r["iters"][i]) - s["iters"]) <= 1, (i, r["iters"][i], s["iters"])
+        assert np.abs(r["q"][i] - s["q"]).max() < 1e-6, i
         ref = O.scc(o, O.kpe_params(M=M, kT=0.01, n_elec=o.n_elec), tol=1e-6, max_iter=100, beta=0.2, history=4)
         assert ref["status"] == 0
         assert np.abs(r["q"][i] - ref["q"]).max() < 2e-6, i
