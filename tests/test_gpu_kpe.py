@@ -66,7 +66,8 @@ def test_density_fp32_matches_oracle(gpu, cfg1):
 @pytest.mark.parametrize("prec", [0, 1])
 def test_step_function_and_autocorr_kernel(gpu, prec):
     m, o = _pair(1, 1, 2, seed=7)
-    for kT, kernel in [(0.0, 0), (0.01, 1), (0.02, 2)]:
+    # kT = 0.002: 16384 quadrature nodes read from a cosine table built for 65536
+    for kT, kernel in [(0.0, 0), (0.01, 1), (0.02, 2), (0.002, 0)]:
         ref = O.density(o, O.kpe_params(M=120, kT=kT, n_elec=o.n_elec, kernel=kernel))
         with _ctx(gpu, m, M=120, kT=kT, kernel=kernel, precision=prec) as c:
             r = c.density()
