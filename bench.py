@@ -211,7 +211,7 @@ def batch_models(T, count=64, seed=4004):
 
 def run_batch_bench(args, T, dev, rank):
     M = 300
-    ms = batch_models(T)
+    ms = batch_models(T)[: args.structures]
     models = [m for _, _, m in ms]
     atoms = np.array([m.natoms for m in models])
     b = T.Batch(models, M=M, device=dev)
@@ -241,12 +241,14 @@ def run_batch_bench(args, T, dev, rank):
             tot_am += atoms[i] * M * s["iters"]
             c.close()
         return tot_am / tot_t, tot_t
-    loop32, t32 = loop(T.PREC_FP32, range(len(models)))
+    loop32 = t32 = loop64 = t64 = None
     sub = [int(i) for i in np.argsort(atoms)[:: max(1, len(models) // 4)][:4]]
-    loop64, t64 = loop(T.PREC_FP64, sub)
+    if not args.no_plain:  # the single-structure loops beside the batch
+        loop32, t32 = loop(T.PREC_FP32, range(len(models)))
+        loop64, t64 = loop(T.PREC_FP64, sub)
     if rank == 0:
         print(json.dumps({
-            "metric": "atoms*moments/s, batched SCC of 64 uneven cristobalite cells (M = 300)",
+            "metric": f"atoms*moments/s, batched SCC of {len(models)} uneven cristobalite cells (M = 300)",
             "value": statistics.mean(am), "unit": "atom-moments/s", "higher_is_better": True,
             "s_per_batch_solve": statistics.mean(ts), "structures": len(models),
             "atoms_total": int(atoms.sum()), "atoms_min": int(atoms.min()), "atoms_max": int(atoms.max()),
@@ -256,8 +258,8 @@ def run_batch_bench(args, T, dev, rank):
                             "timed": "moment phase (steps and per-step finalize), CUDA events"},
             "loop_fp32_single": {"value": loop32, "s_total": t32},
             "loop_plain_fp64_single": {"value": loop64, "structures": sub, "s_total_subset": t64},
-            "speedup_vs_loop_plain_fp64": statistics.mean(am) / loop64,
-            "speedup_vs_loop_fp32": statistics.mean(am) / loop32,
+            "speedup_vs_loop_plain_fp64": statistics.mean(am) / loop64 if loop64 else None,
+            "speedup_vs_loop_fp32": statistics.mean(am) / loop32 if loop32 else None,
             "config": {"dims": [d for d, _, _ in ms], "sigma_ang": [round(sg, 4) for _, sg, _ in ms],
                        "seed": 4004, "M": M, "kT": 0.01, "scc_tol": 1e-6}}), flush=True)
 
@@ -385,7 +387,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells", type=int, nargs=3, default=None)
-    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 solve")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain FP64 solve (with --batch: the single-structure loops)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--column-block", type=int, default=0)
     ap.add_argument("--fp32-kernel", type=int, default=0,
@@ -399,6 +402,8 @@ def main():
                     help="8x8x8 cell (12288 atoms): SCC from q0 vs from the learned start (M = 200)")
     ap.add_argument("--batch", action="store_true",
                     help="64 cristobalite cells of random shape solved as one batch (M = 300)")
+    ap.add_argument("--structures", type=int, default=64,
+                    help="--batch: the first S of the 64 cells (a smaller case for profiling)")
     ap.add_argument("--sp2", action="store_true",
                     help="time SP2 purification of 4x4x4 cristobalite (sigma 0.08 A, drop 1e-5)")
     ap.add_argument("--all-kernels", action="store_true",
