@@ -215,6 +215,16 @@ __device__ __forceinline__ bool wait_neighbours(const PipeArgs &a, int chunk, in
     return true;
 }
 
+// Tile of this CTA's i-th task.  One-launch-per-step launches sweep the
+// tiles backwards on odd steps, so a step starts on the rows of T_{k+1} and
+// T_k that the previous step touched last and that are still in L2.
+__device__ __forceinline__ int tile_of_task(const PipeArgs &a, int ntiles, int i, int mine)
+{
+    const int t = (int)blockIdx.x + (i % mine) * (int)gridDim.x;
+    const int k = a.k0 + i / mine;
+    return (!a.flags && (k & 1)) ? ntiles - 1 - t : t;
+}
+
 // kBatch: tiles come from a.tiles (row groups of many structures, each
 // structure its own chunk-major slabs and partial block); else tile t is
 // (chunk t / G, group t % G) of one slab.
@@ -265,7 +275,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
             if (!wait_phase(&pub[s], (uint32_t)(i / kPubSlots) & 1u, s_abort, a.err)) break;
             if (lane == 0) {
                 const int k = a.k0 + i / mine;
-                const int t = (int)blockIdx.x + (i % mine) * (int)gridDim.x;
+                const int t = tile_of_task(a, ntiles, i, mine);
                 __threadfence();
                 fence_proxy_async_global();
                 st_release(a.flags + t, k + 1);
@@ -284,10 +294,11 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         int64_t cnext = 0;      // batched form: its chunk offset
         if (total > 0) {
             if constexpr (kBatch) {
-                gnext = a.tiles[blockIdx.x].g;
-                cnext = a.tiles[blockIdx.x].coff;
+                const int t0 = tile_of_task(a, ntiles, 0, mine);
+                gnext = a.tiles[t0].g;
+                cnext = a.tiles[t0].coff;
             } else {
-                gnext = (int)blockIdx.x % a.G;
+                gnext = tile_of_task(a, ntiles, 0, mine) % a.G;
             }
             ha = __ldg(a.hdr + 2 * gnext);
             hb = __ldg(a.hdr + 2 * gnext + 1);
@@ -295,7 +306,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         }
         for (; i < total; ++i) {
             const int k = a.k0 + i / mine;
-            const int t = (int)blockIdx.x + (i % mine) * (int)gridDim.x;
+            const int t = tile_of_task(a, ntiles, i, mine);
             const int g = gnext;
             const int chunk = kBatch ? 0 : t / a.G;
             const int64_t coff = kBatch ? cnext : (int64_t)chunk * chunk_floats;
@@ -303,7 +314,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
             const int rl = hb.x, I0 = hb.y, nruns = hb.z, nr = hb.w;
             const int4 cur = run;
             if (i + 1 < total) {  // header and runs of the next tile
-                const int tn = (int)blockIdx.x + ((i + 1) % mine) * (int)gridDim.x;
+                const int tn = tile_of_task(a, ntiles, i + 1, mine);
                 if constexpr (kBatch) {
                     gnext = a.tiles[tn].g;
                     cnext = a.tiles[tn].coff;
@@ -365,7 +376,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
     const int c = 2 * lane;
     for (int i = 0; i < total; ++i) {
         const int k = a.k0 + i / mine;
-        const int t = (int)blockIdx.x + (i % mine) * (int)gridDim.x;
+        const int t = tile_of_task(a, ntiles, i, mine);
         const int s = i % a.stages;
         int g, I0, nr;
         int64_t coff, pbase;  // slab offset of the tile's chunk; float2 offset of its column sums
