@@ -251,9 +251,12 @@ int tb_kpm_dos(tb_ctx *ctx, int32_t n_moments, int32_t n_random, uint64_t seed, 
  * structure keeps its own Gershgorin scaling, chemical potential, Anderson
  * history and convergence test on the device, while every Chebyshev step of
  * all still-unconverged structures runs as one launch (FP32 recurrence, FP64
- * moments; the precision field is ignored).  M, kT, kernel, the SCC
- * tolerance, mixer and iteration cap come from p; n_electrons <= 0 takes
- * sum(q0) per structure. */
+ * moments; the precision field is ignored): the pipelined step kernel over
+ * a tile list of every structure's row groups and column chunks, or, with
+ * fp32_kernel = TB_FP32_STAGED (or when a pipeline stage does not fit in
+ * shared memory), the staged one.  M, kT, kernel, the SCC tolerance, mixer
+ * and iteration cap come from p; n_electrons <= 0 takes sum(q0) per
+ * structure. */
 typedef struct tb_batch tb_batch;
 
 int tb_batch_create(const tb_params *p, int32_t count, tb_batch **out);
