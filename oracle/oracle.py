@@ -141,6 +141,9 @@ def lib():
         L.orc_sp2.argtypes = [
             C.c_int, i32p, i32p, f64p, i32p, C.c_int, C.POINTER(OrcSp2Params), f64p, f64p,
             i32p, f64p, f64p, C.POINTER(OrcSp2Result)]
+        L.orc_anderson.argtypes = [
+            C.c_int, f64p, f64p, C.c_double, C.c_int, f64p, f64p, C.POINTER(C.c_int),
+            C.POINTER(C.c_int), f64p]
         L.orc_kpm_dos.argtypes = [
             C.c_int, i32p, i32p, f64p, C.c_double, C.c_double, C.c_int, C.c_int, C.c_uint64,
             C.c_int, f64p, f64p, f64p]
@@ -377,6 +380,69 @@ def scc(m: Model, p: OrcKpeParams, tol=1e-6, max_iter=100, beta=0.3, history=6, 
     return dict(status=rc, q=q, diagP=diagP, iters=it.value, dq_hist=hist[: it.value],
                 e_band=res.e_band, mu=res.mu, mu_x=res.mu_x, a=res.a, b=res.b)
 
+
+class Anderson:
+    """The oracle's Anderson mixer (orc_anderson) with its ring of past
+    (q_in, residual) pairs held here, so a caller can run orc_scc's loop one
+    density evaluation at a time and save or restore the mixer between them."""
+
+    def __init__(self, natoms, beta=0.2, history=16):
+        self.natoms, self.beta, self.history = natoms, beta, history
+        h = max(history, 1)
+        self.hq = np.zeros(h * natoms)
+        self.hr = np.zeros(h * natoms)
+        self.count, self.head = C.c_int(0), C.c_int(0)
+
+    def step(self, q_in, r):
+        out = np.zeros(self.natoms)
+        _check(lib().orc_anderson(self.natoms, np.ascontiguousarray(q_in, np.float64),
+                                  np.ascontiguousarray(r, np.float64), self.beta, self.history,
+                                  self.hq, self.hr, C.byref(self.count), C.byref(self.head), out),
+               "anderson")
+        return out
+
+    def state(self):
+        return dict(hq=self.hq.copy(), hr=self.hr.copy(), count=self.count.value,
+                    head=self.head.value)
+
+    def restore(self, st):
+        self.hq[:] = st["hq"]
+        self.hr[:] = st["hr"]
+        self.count.value, self.head.value = int(st["count"]), int(st["head"])
+
+
+class SccLoop:
+    """orc_scc's loop (withSP2_deltaH.cpp:1820-1840 made to converge) one
+    density evaluation at a time: the same C routines in the same order, so
+    its iterates are bit-identical to orc_scc's.  step() evaluates the density
+    at the current input charges, records the residual, mixes, and returns
+    (iteration, q_in, density result, max |q_out - q_in|).  state()/restore()
+    save and reload everything the next step depends on."""
+
+    def __init__(self, m: Model, p: OrcKpeParams, beta=0.2, history=16, q_init=None):
+        self.m, self.p = m, p
+        self.mix = Anderson(m.natoms, beta, history)
+        self.it = 0
+        self.q_in = np.array(m.q0 if q_init is None else q_init, np.float64)
+
+    def step(self, mix=True):
+        m = self.m
+        self.it += 1
+        V = gamma_mult(m, self.q_in - m.q0)
+        r = density(m, self.p, shift=V[m.orb2atom])
+        res = r["q"] - self.q_in
+        q_in = self.q_in
+        if mix:
+            self.q_in = self.mix.step(q_in, res)
+        return self.it, q_in, r, float(np.abs(res).max())
+
+    def state(self):
+        return dict(it=self.it, q_in=self.q_in.copy(), **self.mix.state())
+
+    def restore(self, st):
+        self.it = int(st["it"])
+        self.q_in = np.array(st["q_in"], np.float64)
+        self.mix.restore(st)
 
 def sp2(m: Model, drop_tol=1e-5, max_iter=40, idem_tol=1e-10, trace_tol=0.0, nthreads=0):
     """Thresholded block SP2 (getSP2/computeAlphas restated as matrix purification)."""
