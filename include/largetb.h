@@ -337,10 +337,14 @@ int tb_abi_version(void);
  * process exits.  d_rowptr (n+1), d_colidx and d_vals (nnz) and d_moments
  * (M+1) are device pointers owned by the caller; d_moments is cleared and
  * overwritten.  `stream` is a cudaStream_t (NULL: the legacy default stream);
- * the call returns after the stream has finished the work.
+ * the call ends with a cudaStreamSynchronize of `stream`, so it returns after
+ * the stream has finished the work.
  *   - The first call on a device looks up the scratch array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *     (cudaGetSymbolAddress) with that device current, and looks it up again
+ *     when the device's context has changed (after a cudaDeviceReset); make
+ *     that first call before any stream capture.
+ *   - A CUDA error already pending on entry returns TB_ERR_CUDA before any
+ *     work is queued and is left pending for the caller.
  *   - Every call shares the one scratch array: calls that overlap on the GPU
  *     (from several host threads or streams) race and give wrong results.
  *   - n > TB_NOALLOC_MAX_N returns TB_ERR_UNSUPPORTED without touching the

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libtb_gb300.so")
 SOURCES = ["tb_api.cpp", "tb_model.cpp", "tb_kpe.cu", "tb_sp2.cu", "tb_dos.cu", "tb_batch.cu", "tb_geom.cu", "tb_mlp.cu", "tb_noalloc.cu", "tb_pipe.cu", "tb_mlp_tc.cu"]
-HEADERS = ["tb_internal.h", "tb_f32x2.cuh", os.path.join("..", "..", "include", "largetb.h")]
+HEADERS = ["tb_internal.h", "tb_abi_guard.h", "tb_f32x2.cuh", os.path.join("..", "..", "include", "largetb.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1315,6 +1315,7 @@ const char *tb_status_string(int s)
 
 int tb_params_init(tb_params *p)
 {
+    TB_ABI_TRY
     if (!p) return TB_ERR_INVALID_ARG;
     std::memset(p, 0, sizeof(*p));
     p->struct_size = sizeof(tb_params);
@@ -1335,10 +1336,12 @@ int tb_params_init(tb_params *p)
     p->sp2_max_iter = 40;
     p->sp2_idem_tol = 1e-10;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_ctx_create(const tb_params *p, tb_ctx **out)
 {
+    TB_ABI_TRY
     if (!out) return TB_ERR_INVALID_ARG;
     *out = nullptr;
     int rc = check_params(nullptr, p);
@@ -1362,10 +1365,12 @@ int tb_ctx_create(const tb_params *p, tb_ctx **out)
     }
     *out = ctx;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_ctx_destroy(tb_ctx *ctx)
 {
+    TB_ABI_TRY
     if (!ctx) return TB_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -1380,10 +1385,12 @@ int tb_ctx_destroy(tb_ctx *ctx)
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_set_params(tb_ctx *ctx, const tb_params *p)
 {
+    TB_ABI_TRY
     if (!ctx) return TB_ERR_INVALID_ARG;
     ctx->gen++;
     TB_TRY(check_params(ctx, p));
@@ -1392,13 +1399,16 @@ int tb_set_params(tb_ctx *ctx, const tb_params *p)
     ctx->p = *p;
     if (!(p->n_electrons > 0) && ctx->have_scc) ctx->p.n_electrons = ne;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_get_params(const tb_ctx *ctx, tb_params *p)
 {
+    TB_ABI_TRY
     if (!ctx || !p) return TB_ERR_INVALID_ARG;
     *p = ctx->p;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 const char *tb_last_error(const tb_ctx *ctx)
@@ -1410,6 +1420,7 @@ const char *tb_last_error(const tb_ctx *ctx)
 int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int32_t *colidx,
                        const double *vals, const int32_t *orb2atom, int32_t natoms)
 {
+    TB_ABI_TRY
     if (!ctx) return TB_ERR_INVALID_ARG;
     ctx->gen++;
     HostBsr hb;
@@ -1441,11 +1452,13 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
     ctx->asym_max = hb.asym;
     ctx->have_h = true;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_set_geometry(tb_ctx *ctx, int32_t natoms, const double *xyz, const int32_t *species,
                     const double *box, double rcut_bohr, double gamma_diag)
 {
+    TB_ABI_TRY
     if (!ctx) return TB_ERR_INVALID_ARG;
     ctx->gen++;
     if (natoms <= 0 || !xyz || !species || !box || !(rcut_bohr > 0) || !std::isfinite(gamma_diag))
@@ -1509,11 +1522,13 @@ int tb_set_geometry(tb_ctx *ctx, int32_t natoms, const double *xyz, const int32_
     TB_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->have_h = ctx->have_scc = true;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_set_scc(tb_ctx *ctx, int32_t natoms, const int32_t *g_rowptr, const int32_t *g_colidx,
                const double *g_vals, const double *q0)
 {
+    TB_ABI_TRY
     if (!ctx) return TB_ERR_INVALID_ARG;
     ctx->gen++;
     if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "tb_set_hamiltonian must come first");
@@ -1542,10 +1557,12 @@ int tb_set_scc(tb_ctx *ctx, int32_t natoms, const int32_t *g_rowptr, const int32
     TB_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->have_scc = true;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_gershgorin(tb_ctx *ctx, const double *shift, double *lmin, double *lmax)
 {
+    TB_ABI_TRY
     if (!ctx || !lmin || !lmax) return TB_ERR_INVALID_ARG;
     if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian not set");
     TB_TRY(set_device(ctx));
@@ -1560,11 +1577,13 @@ int tb_gershgorin(tb_ctx *ctx, const double *shift, double *lmin, double *lmax)
     *lmin = hs.lmin;
     *lmax = hs.lmax;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_density(tb_ctx *ctx, const double *shift, double *diagP, double *q, double *e_band,
                double *mu, double *moments, tb_report *rep)
 {
+    TB_ABI_TRY
     if (!ctx) return TB_ERR_INVALID_ARG;
     if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian not set");
     if (!(ctx->p.n_electrons > 0))
@@ -1609,10 +1628,12 @@ int tb_density(tb_ctx *ctx, const double *shift, double *diagP, double *q, doubl
         rep->fp32_check_ms = chk_ms;
     }
     return rc;
+    TB_ABI_CATCH
 }
 
 int tb_coulomb_shift(tb_ctx *ctx, const double *q, double *V)
 {
+    TB_ABI_TRY
     if (!ctx || !q || !V) return TB_ERR_INVALID_ARG;
     if (!ctx->have_scc) return fail(ctx, TB_ERR_NOT_READY, "SCC data not set");
     TB_TRY(set_device(ctx));
@@ -1623,11 +1644,13 @@ int tb_coulomb_shift(tb_ctx *ctx, const double *q, double *V)
     TB_CUDA(cudaMemcpyAsync(V, ctx->s.V, na * 8, cudaMemcpyDeviceToHost, ctx->stream));
     TB_CUDA(cudaStreamSynchronize(ctx->stream));
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, double *e_band,
                  double *mu, int32_t *iters, tb_report *rep)
 {
+    TB_ABI_TRY
     if (!ctx) return TB_ERR_INVALID_ARG;
     if (!ctx->have_h || !ctx->have_scc)
         return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian and SCC data must be set");
@@ -1688,10 +1711,12 @@ int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, do
     if (iters) *iters = it;
     fill_report(ctx, e0, hs, it, rep);
     return rc;
+    TB_ABI_CATCH
 }
 
 int tb_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep)
 {
+    TB_ABI_TRY
     if (!ctx) return TB_ERR_INVALID_ARG;
     if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian not set");
     if (!(ctx->p.n_electrons > 0))
@@ -1714,11 +1739,13 @@ int tb_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep
     r.asym_max = ctx->asym_max;
     if (rep) *rep = r;
     return rc;
+    TB_ABI_CATCH
 }
 
 int tb_kpm_dos(tb_ctx *ctx, int32_t n_moments, int32_t n_random, uint64_t seed, int32_t npts,
                double *moments, double *energies, double *dos, tb_report *rep)
 {
+    TB_ABI_TRY
     if (!ctx) return TB_ERR_INVALID_ARG;
     if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian not set");
     if (n_moments < 2 || n_moments > 100000 || n_random < 1 || n_random > 4096 || npts < 1 ||
@@ -1750,6 +1777,7 @@ int tb_kpm_dos(tb_ctx *ctx, int32_t n_moments, int32_t n_random, uint64_t seed, 
         rep->precision = TB_PREC_FP64;
     }
     return rc;
+    TB_ABI_CATCH
 }
 
 }  // extern "C"

@@ -984,6 +984,7 @@ extern "C" {
 
 int tb_batch_create(const tb_params *p, int32_t count, tb_batch **out)
 {
+    TB_ABI_TRY
     if (!out || !p || count < 1) return TB_ERR_INVALID_ARG;
     *out = nullptr;
     if (p->struct_size != sizeof(tb_params) || p->M < 2 || p->M > 6000 || p->mix_history < 0 ||
@@ -1015,10 +1016,12 @@ int tb_batch_create(const tb_params *p, int32_t count, tb_batch **out)
     }
     *out = b;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_batch_destroy(tb_batch *b)
 {
+    TB_ABI_TRY
     if (!b) return TB_OK;
     cudaSetDevice(b->p.device);
     if (b->stream) cudaStreamSynchronize(b->stream);
@@ -1029,6 +1032,7 @@ int tb_batch_destroy(tb_batch *b)
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 const char *tb_batch_last_error(const tb_batch *b) { return b ? b->err.c_str() : "no batch"; }
@@ -1037,6 +1041,7 @@ int tb_batch_set(tb_batch *b, int32_t index, int32_t n, const int32_t *rowptr, c
                  const double *vals, int32_t natoms, const int32_t *g_rowptr, const int32_t *g_colidx,
                  const double *g_vals, const double *q0)
 {
+    TB_ABI_TRY
     if (!b) return TB_ERR_INVALID_ARG;
     if (index < 0 || index >= b->S) return bfail(b, TB_ERR_INVALID_ARG, "index out of range");
     std::vector<int32_t> o2a(n > 0 ? n : 0);
@@ -1053,11 +1058,13 @@ int tb_batch_set(tb_batch *b, int32_t index, int32_t n, const int32_t *rowptr, c
     b->have[index] = 1;
     b->built = false;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *iters, double *e_band,
                        double *mu, tb_report *rep)
 {
+    TB_ABI_TRY
     if (!b) return TB_ERR_INVALID_ARG;
     for (int s = 0; s < b->S; s++)
         if (!b->have[s]) return bfail(b, TB_ERR_NOT_READY, "structure " + std::to_string(s) + " not set");
@@ -1309,6 +1316,7 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
         rep->column_block = -1;
     }
     return rc;
+    TB_ABI_CATCH
 }
 
 }  // extern "C"

@@ -5,10 +5,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <new>
 #include <string>
 #include <vector>
 
 #include "../../include/largetb.h"
+#include "tb_abi_guard.h"
 
 namespace tb {
 

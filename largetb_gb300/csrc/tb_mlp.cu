@@ -314,6 +314,7 @@ extern "C" {
 
 int tb_mlp_features(int32_t natoms, const double *xyz, const int32_t *species, const double *box, float *feat)
 {
+    TB_ABI_TRY
     if (natoms <= 0 || !xyz || !species || !box || !feat) return TB_ERR_INVALID_ARG;
     double *dx = nullptr;
     int32_t *ds = nullptr;
@@ -333,10 +334,12 @@ int tb_mlp_features(int32_t natoms, const double *xyz, const int32_t *species, c
     cudaFree(ds);
     cudaFree(df);
     return rc;
+    TB_ABI_CATCH
 }
 
 int tb_mlp_create(int32_t device, uint64_t seed, tb_mlp **out)
 {
+    TB_ABI_TRY
     if (!out) return TB_ERR_INVALID_ARG;
     *out = nullptr;
     int ndev = 0;
@@ -376,10 +379,12 @@ int tb_mlp_create(int32_t device, uint64_t seed, tb_mlp **out)
     }
     *out = m;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_mlp_destroy(tb_mlp *m)
 {
+    TB_ABI_TRY
     if (!m) return TB_OK;
     cudaSetDevice(m->device);
     if (m->stream) cudaStreamSynchronize(m->stream);
@@ -395,10 +400,12 @@ int tb_mlp_destroy(tb_mlp *m)
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_mlp_get(const tb_mlp *m, float *params, float *norm)
 {
+    TB_ABI_TRY
     if (!m) return TB_ERR_INVALID_ARG;
     cudaSetDevice(m->device);
     if (params && cudaMemcpy(params, m->W, sizeof(float) * kNP, cudaMemcpyDeviceToHost)) return TB_ERR_CUDA;
@@ -406,10 +413,12 @@ int tb_mlp_get(const tb_mlp *m, float *params, float *norm)
                  cudaMemcpy(norm + kF, m->istd, sizeof(float) * kF, cudaMemcpyDeviceToHost)))
         return TB_ERR_CUDA;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_mlp_set(tb_mlp *m, const float *params, const float *norm)
 {
+    TB_ABI_TRY
     if (!m) return TB_ERR_INVALID_ARG;
     cudaSetDevice(m->device);
     if (params) {
@@ -424,10 +433,12 @@ int tb_mlp_set(tb_mlp *m, const float *params, const float *norm)
         m->have_norm = true;
     }
     return cudaStreamSynchronize(m->stream) == cudaSuccess ? TB_OK : TB_ERR_CUDA;
+    TB_ABI_CATCH
 }
 
 int tb_mlp_grad(tb_mlp *m, int32_t n, const float *feat, const float *target, float *grad, float *loss)
 {
+    TB_ABI_TRY
     if (!m || n <= 0 || !feat || !target || !grad) return TB_ERR_INVALID_ARG;
     cudaSetDevice(m->device);
     float *dX, *dT;
@@ -444,10 +455,12 @@ int tb_mlp_grad(tb_mlp *m, int32_t n, const float *feat, const float *target, fl
     cudaFree(dX);
     cudaFree(dT);
     return rc;
+    TB_ABI_CATCH
 }
 
 int tb_mlp_predict(tb_mlp *m, int32_t n, const float *feat, float *out)
 {
+    TB_ABI_TRY
     if (!m || n <= 0 || !feat || !out) return TB_ERR_INVALID_ARG;
     cudaSetDevice(m->device);
     float *dX = nullptr, *dY = nullptr;
@@ -467,10 +480,12 @@ int tb_mlp_predict(tb_mlp *m, int32_t n, const float *feat, float *out)
     cudaFree(dX);
     cudaFree(dY);
     return rc;
+    TB_ABI_CATCH
 }
 
 int tb_mlp_predict_fp32(tb_mlp *m, int32_t n, const float *feat, float *out)
 {
+    TB_ABI_TRY
     if (!m || n <= 0 || !feat || !out) return TB_ERR_INVALID_ARG;
     cudaSetDevice(m->device);
     float *dX = nullptr, *dY = nullptr;
@@ -485,11 +500,13 @@ int tb_mlp_predict_fp32(tb_mlp *m, int32_t n, const float *feat, float *out)
     cudaFree(dX);
     cudaFree(dY);
     return rc;
+    TB_ABI_CATCH
 }
 
 int tb_mlp_train(tb_mlp *m, int32_t n, const float *feat, const float *target, int32_t epochs, int32_t batch,
                  float lr, uint64_t seed, float *loss_per_epoch)
 {
+    TB_ABI_TRY
     if (!m || n <= 0 || !feat || !target || epochs < 1 || batch < 1 || !(lr > 0)) return TB_ERR_INVALID_ARG;
     cudaSetDevice(m->device);
     cudaStream_t st = m->stream;
@@ -547,6 +564,7 @@ int tb_mlp_train(tb_mlp *m, int32_t n, const float *feat, const float *target, i
     cudaFree(dT);
     cudaFree(dI);
     return rc;
+    TB_ABI_CATCH
 }
 
 }  // extern "C"

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/largetb.h"
+#include "tb_abi_guard.h"
 
 namespace {
 
@@ -199,6 +200,7 @@ extern "C" {
 
 int tb_model_quartz(int32_t L, int32_t M, int32_t N, tb_model **out)
 {
+    TB_ABI_TRY
     if (!out || L < 1 || M < 1 || N < 1) return TB_ERR_INVALID_ARG;
     *out = nullptr;
     tb_model *m = new (std::nothrow) tb_model();
@@ -252,11 +254,13 @@ int tb_model_quartz(int32_t L, int32_t M, int32_t N, tb_model **out)
     }
     *out = m;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_model_cristobalite(int32_t nx, int32_t ny, int32_t nz, double a_ang, double sigma_ang,
                           uint64_t seed, double rcut_bohr, double gamma_diag, tb_model **out)
 {
+    TB_ABI_TRY
     if (!out || nx < 1 || ny < 1 || nz < 1 || !(a_ang > 0) || !(sigma_ang >= 0) || !(rcut_bohr > 0) ||
         !std::isfinite(gamma_diag))
         return TB_ERR_INVALID_ARG;
@@ -346,22 +350,26 @@ int tb_model_cristobalite(int32_t nx, int32_t ny, int32_t nz, double a_ang, doub
     }
     *out = m;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_model_sizes(const tb_model *m, int32_t *natoms, int32_t *n, int64_t *nnz, int64_t *g_nnz)
 {
+    TB_ABI_TRY
     if (!m) return TB_ERR_INVALID_ARG;
     if (natoms) *natoms = m->natoms;
     if (n) *n = 4 * m->natoms;
     if (nnz) *nnz = (int64_t)m->vals.size();
     if (g_nnz) *g_nnz = (int64_t)m->g_vals.size();
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_model_export(const tb_model *m, int32_t *rowptr, int32_t *colidx, double *vals,
                     int32_t *orb2atom, int32_t *g_rowptr, int32_t *g_colidx, double *g_vals,
                     double *q0, double *xyz, int32_t *species)
 {
+    TB_ABI_TRY
     if (!m) return TB_ERR_INVALID_ARG;
     const size_t n = 4 * (size_t)m->natoms;
     if (rowptr) std::memcpy(rowptr, m->rowptr.data(), (n + 1) * sizeof(int32_t));
@@ -376,12 +384,15 @@ int tb_model_export(const tb_model *m, int32_t *rowptr, int32_t *colidx, double 
     if (xyz) std::memcpy(xyz, m->xyz.data(), m->xyz.size() * sizeof(double));
     if (species) std::memcpy(species, m->species.data(), m->species.size() * sizeof(int32_t));
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 int tb_model_destroy(tb_model *m)
 {
+    TB_ABI_TRY
     delete m;
     return TB_OK;
+    TB_ABI_CATCH
 }
 
 }  // extern "C"

@@ -27,7 +27,31 @@ constexpr int kNoAllocWarps = 8;
 static __device__ __align__(256) double g_noalloc_slabs[2 * TB_NOALLOC_MAX_N * kNoAllocCols];
 
 std::mutex g_setup_mu;
-double *g_slab_ptr[64] = {nullptr};  // device address of the array, per device ordinal
+// Device address of the array, per device ordinal, with the context it was
+// looked up in: after a cudaDeviceReset (or under another driver context) the
+// cached address would be stale, so a different current context repeats the
+// lookup.
+double *g_slab_ptr[64] = {nullptr};
+void *g_slab_ctx[64] = {nullptr};
+
+// The current driver context (the runtime API has no query of its own);
+// nullptr when the entry point cannot be resolved.
+void *current_context()
+{
+    using get_fn = int (*)(void **);
+    static get_fn fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<get_fn>(f);
+    }();
+    void *ctx = nullptr;
+    if (fn && fn(&ctx) != 0) ctx = nullptr;
+    return ctx;
+}
 
 // T0 = E[:, c0:c0+64] and mu_0 += (columns in range).
 __global__ void k_noalloc_identity(double *__restrict__ T0, int n, int c0, double *__restrict__ mom)
@@ -99,23 +123,31 @@ extern "C" int tb_moments_noalloc(int32_t n, const int32_t *d_rowptr, const int3
                                   const double *d_vals, double a, double b, int32_t M,
                                   double *d_moments, void *stream)
 {
+    TB_ABI_TRY
     if (n <= 0 || M < 1 || !(a > 0) || !d_rowptr || !d_colidx || !d_vals || !d_moments)
         return TB_ERR_INVALID_ARG;
     if (n > TB_NOALLOC_MAX_N) return TB_ERR_UNSUPPORTED;  // beyond the static scratch
+    // An error the caller left pending is theirs: report it before queueing
+    // anything, and leave it in place.
+    if (cudaPeekAtLastError() != cudaSuccess) return TB_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TB_ERR_NO_DEVICE;
     double *slabs = nullptr;
     {
-        // once per device, with that device current: the address of the
-        // file-scope array (its host-side name is only a stand-in)
+        // set-up, once per device (again if its context changed), with that
+        // device current: the device address of the file-scope array, whose
+        // host-side name is only a stand-in
         std::lock_guard<std::mutex> lk(g_setup_mu);
-        if (!g_slab_ptr[dev]) {
+        void *ctx = current_context();
+        if (!g_slab_ptr[dev] || ctx != g_slab_ctx[dev]) {
             void *p = nullptr;
             if (cudaGetSymbolAddress(&p, g_noalloc_slabs) != cudaSuccess || !p) {
                 cudaGetLastError();
+                g_slab_ptr[dev] = nullptr;
                 return TB_ERR_CUDA;
             }
             g_slab_ptr[dev] = static_cast<double *>(p);
+            g_slab_ctx[dev] = ctx;
         }
         slabs = g_slab_ptr[dev];
     }
@@ -132,8 +164,13 @@ extern "C" int tb_moments_noalloc(int32_t n, const int32_t *d_rowptr, const int3
                                                                 odd ? A : Bf, odd ? Bf : A, c0,
                                                                 kout == 1, d_moments, kout);
         }
+        // a failed launch stops the loop at the end of its slab
+        if (cudaGetLastError() != cudaSuccess) {
+            cudaStreamSynchronize(st);
+            return TB_ERR_CUDA;
+        }
     }
-    if (cudaGetLastError() != cudaSuccess) return TB_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return TB_ERR_CUDA;
     return TB_OK;
+    TB_ABI_CATCH
 }

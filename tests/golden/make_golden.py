@@ -1,6 +1,6 @@
 """Convert the reference's own matrix/vector dumps into compact fixtures.
 
-Reads, from a checkout of pghale/largeTB (default /root/reference), the
+Reads, from a checkout of pghale/largeTB (its path is the first argument), the
 PETSc MATLAB-format dumps the reference wrote (MatView/VecView with
 PETSC_VIEWER_ASCII_MATLAB) and the Jackson table of runKPM, and writes
 tests/golden/reference_dumps.npz:
@@ -63,7 +63,7 @@ def read_vec(path):
     return np.array(out)
 
 
-def main(ref="/root/reference", out=None):
+def main(ref, out=None):
     out = out or os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_dumps.npz")
     d = {}
     for key, name in [("amat", "Amat.m"), ("h444", "H.m"), ("gamma", "GAMMA_AB.m"),
@@ -81,4 +81,6 @@ def main(ref="/root/reference", out=None):
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: make_golden.py REFERENCE_CHECKOUT [OUT.npz]")
     main(*sys.argv[1:])
