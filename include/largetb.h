@@ -152,7 +152,9 @@ typedef struct tb_report {
     double fp32_diag_err;     /* with check_fp32: max |diagP(FP32) - diagP(FP64)| over the
                                  checked orbitals, else 0 */
     double fp32_check_ms;     /* CUDA-event time of that check */
-    double reserved[4];
+    double sp2_flops_done;    /* SP2: 128 x block products actually formed (the symmetric
+                                 product forms the blocks J >= I only) */
+    double reserved[3];
 } tb_report;
 
 typedef struct tb_ctx tb_ctx;

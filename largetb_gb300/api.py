@@ -107,7 +107,8 @@ class TbReport(C.Structure):
         ("sp2_bytes", C.c_double),
         ("fp32_diag_err", C.c_double),
         ("fp32_check_ms", C.c_double),
-        ("reserved", C.c_double * 4),
+        ("sp2_flops_done", C.c_double),
+        ("reserved", C.c_double * 3),
     ]
 
     def as_dict(self):
