@@ -49,7 +49,9 @@ enum tb_status {
     TB_ERR_CUDA = 9,          /* CUDA runtime error; message in tb_last_error */
     TB_ERR_NO_DEVICE = 10,    /* no CUDA device of compute capability 10.3 */
     TB_ERR_OUT_OF_MEMORY = 11,
-    TB_ERR_UNSUPPORTED = 12
+    TB_ERR_UNSUPPORTED = 12,
+    TB_ERR_TIMEOUT = 13       /* a bounded device wait ran out: the kernel stopped early and
+                                 returned; results of the call are void, the context stays usable */
 };
 
 enum tb_precision {

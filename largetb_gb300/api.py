@@ -34,6 +34,7 @@ TB_ERR_CUDA = 9
 TB_ERR_NO_DEVICE = 10
 TB_ERR_OUT_OF_MEMORY = 11
 TB_ERR_UNSUPPORTED = 12
+TB_ERR_TIMEOUT = 13
 
 PREC_FP64 = 0
 PREC_FP32 = 1

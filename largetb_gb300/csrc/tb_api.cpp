@@ -160,11 +160,13 @@ int check_kernel_flags(tb_ctx *ctx)
     TB_CUDA(cudaStreamSynchronize(ctx->stream));
     if (perr) {
         cudaMemsetAsync(ctx->pp.err, 0, sizeof(int32_t), ctx->stream);
-        return fail(ctx, TB_ERR_CUDA, "persistent Chebyshev kernel: neighbour wait timed out");
+        return fail(ctx, TB_ERR_TIMEOUT, "persistent Chebyshev kernel: a neighbour-flag wait ran out");
     }
     if (serr) {
         cudaMemsetAsync(ctx->pl.err, 0, sizeof(int32_t), ctx->stream);
-        return fail(ctx, TB_ERR_CUDA, "pipelined Chebyshev kernel: stage wait timed out");
+        if (serr == 3) return fail(ctx, TB_ERR_CUDA, "pipelined Chebyshev kernel: a stage held a foreign record");
+        return fail(ctx, TB_ERR_TIMEOUT, serr == 2 ? "pipelined Chebyshev kernel: a neighbour-flag wait ran out"
+                                                   : "pipelined Chebyshev kernel: a stage mbarrier wait ran out");
     }
     return TB_OK;
 }
@@ -1309,6 +1311,7 @@ const char *tb_status_string(int s)
     case TB_ERR_NO_DEVICE: return "no sm_103 CUDA device";
     case TB_ERR_OUT_OF_MEMORY: return "out of device memory";
     case TB_ERR_UNSUPPORTED: return "unsupported";
+    case TB_ERR_TIMEOUT: return "a bounded device wait ran out";
     default: return "unknown status";
     }
 }

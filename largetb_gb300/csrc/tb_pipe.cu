@@ -57,10 +57,18 @@
 // CTA then returns at once, the warps run out their tile sequence skipping
 // the work, other CTAs waiting on this one's flags time out the same way, and the
 // producer, before it returns, waits (again bounded) for the copies it has
-// issued.
+// issued.  The host turns the error flag into TB_ERR_TIMEOUT (1: a stage
+// mbarrier wait, 2: a neighbour-flag wait ran out).
+//
+// Two environment variables, read at each one-launch-per-slab launch, let a
+// test make a neighbour wait run out without any fault: LARGETB_TEST_WAIT_LIMIT
+// (neighbour-flag polls before giving up; default 2^22) and
+// LARGETB_TEST_STALL_TILE (a tile whose step flags are never published, so
+// every tile that reads its rows waits for a flag that nothing sets).
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "tb_f32x2.cuh"
 #include "tb_internal.h"
@@ -92,6 +100,8 @@ struct PipeArgs {
     int32_t *err;
     const PipeBatchTile *tiles;  // batched form: the tile list (slab and partial offsets per tile)
     int ntiles;
+    uint32_t flag_spin;  // neighbour-flag polls before a wait gives up (kFlagSpin unless a test lowers it)
+    int stall_tile;      // test knob: this tile never publishes its step flags (-1: none)
 };
 
 __device__ __forceinline__ uint32_t sm_addr(const void *p)
@@ -159,17 +169,50 @@ __device__ __forceinline__ void fence_proxy_async_global()
     asm volatile("fence.proxy.async.global;\n" ::: "memory");
 }
 
-// Poll until the phase of the given parity completes; false on abort or
-// after kPipeSpin polls (then the abort and device error flags are raised).
+// Warp-collective (every lane of the warp calls it, all get the same
+// answer): poll until the phase of the given parity completes; false on abort
+// or after kPipeSpin polls (then the abort and device error flags are
+// raised).  The abort test is a warp vote, so a warp never splits over it.
 __device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity, volatile int *s_abort,
                                            int32_t *err)
 {
     uint32_t n = 0;
-    while (!mbar_try_wait(bar, parity)) {
-        if (*s_abort) return false;
+    while (!__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) {
+        if (__any_sync(0xffffffffu, *s_abort != 0)) return false;
         if (++n >= kPipeSpin) {
-            *s_abort = 1;
-            atomicExch(err, 1);
+            if ((threadIdx.x & 31) == 0) {
+                *s_abort = 1;
+                atomicExch(err, 1);
+            }
+            __syncwarp();
+            return false;
+        }
+    }
+    return true;
+}
+
+// Warp-collective wait of the consumers for tile i's stage.  A tile the
+// producer issued is always waited for (its bulk copies must land before the
+// stage is refilled or the CTA exits), abort or not; a tile the producer never
+// issued (*s_issued: -1 while it runs, then the count it issued) is given up.
+// That test comes before the barrier poll: once the consumers pass over a
+// phase that never completed, a later poll of the same stage can name a
+// parity that an older, completed phase had, and try_wait would report the
+// never-filled stage as full.  Bounded by kPipeSpin polls like every wait.
+__device__ __forceinline__ bool wait_full(uint64_t *bar, uint32_t parity, int i, volatile int *s_abort,
+                                          volatile int *s_issued, int32_t *err)
+{
+    uint32_t n = 0;
+    for (;;) {
+        const int iss = __shfl_sync(0xffffffffu, *s_issued, 0);
+        if (iss >= 0 && i >= iss) return false;
+        if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
+        if (++n >= kPipeSpin) {
+            if ((threadIdx.x & 31) == 0) {
+                *s_abort = 1;
+                atomicExch(err, 1);
+            }
+            __syncwarp();
             return false;
         }
     }
@@ -200,8 +243,8 @@ __device__ __forceinline__ bool wait_neighbours(const PipeArgs &a, int chunk, in
         const int32_t *f = q < p1 ? fl + a.nbr[q] : nullptr;
         uint32_t n = 0;
         while (!__all_sync(0xffffffffu, f == nullptr || ld_acquire(f) >= k)) {
-            if (*s_abort) return false;
-            if (++n >= kFlagSpin) {
+            if (__any_sync(0xffffffffu, *s_abort != 0)) return false;
+            if (++n >= a.flag_spin) {
                 if (lane == 0) {
                     *s_abort = 1;
                     atomicExch(a.err, 2);
@@ -240,6 +283,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
     uint64_t *redfull = pubfree + kPubSlots;  // consumer warps -> reducers: red[] holds the tile's sums
     uint64_t *redfree = redfull + 1;          // reducers -> consumer warps: red[] read
     volatile int *s_abort = reinterpret_cast<volatile int *>(redfree + 1);
+    volatile int *s_issued = s_abort + 1;  // tiles the producer issued, -1 while it runs
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         for (int s = 0; s < a.stages; s++) {
@@ -253,6 +297,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         mbar_init(redfull, kPipeCW);
         mbar_init(redfree, kRedWarps);
         *s_abort = 0;
+        *s_issued = -1;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
@@ -278,7 +323,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                 const int t = tile_of_task(a, ntiles, i, mine);
                 __threadfence();
                 fence_proxy_async_global();
-                st_release(a.flags + t, k + 1);
+                if (t != a.stall_tile) st_release(a.flags + t, k + 1);
                 mbar_arrive(&pubfree[s]);
             }
             __syncwarp();
@@ -338,6 +383,8 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                 if (!wait_neighbours(a, chunk, g, k, lane, seen, s_abort)) break;
                 fence_proxy_async_global();
             }
+            // no copy is issued once any warp of the CTA has given up
+            if (__any_sync(0xffffffffu, *s_abort != 0)) break;
             const float *Tin = (k & 1) ? a.T1 : a.T0;
             const float *Tprev = (k & 1) ? a.T0 : a.T1;
             float *stg = reinterpret_cast<float *>(smem + (size_t)s * a.stage_bytes);
@@ -360,6 +407,12 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                 if (k > 0)
                     bulk_g2s(stg + oP, Tprev + coff + (int64_t)I0 * 4 * kPipeCols, (uint32_t)nr * 1024u, &full[s]);
             }
+        }
+        // the consumers wait for every tile issued (i of them) and give up the rest
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            *s_issued = i;
         }
         if (*s_abort) {
             // let the copies already issued land before the CTA exits
@@ -400,13 +453,16 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         // pairs (hi, lo), packed over columns (c, c+1): <T_k,T_k> in (eh, el),
         // <T_k,T_{k+1}> in (oh, ol)
         float2 eh = make_float2(0.f, 0.f), el = eh, oh = eh, ol = eh;
-        if (wait_phase(&full[s], (uint32_t)(i / a.stages) & 1u, s_abort, a.err)) {
+        if (wait_full(&full[s], (uint32_t)(i / a.stages) & 1u, i, s_abort, s_issued, a.err)) {
             const float *stg = reinterpret_cast<const float *>(smem + (size_t)s * a.stage_bytes);
             const float *sT = stg + oT, *sP = stg + oP, *sX = stg + oX;
             const int32_t *sRp = reinterpret_cast<const int32_t *>(stg + oRec);
             const int32_t *sLc = sRp + nr + 1;
             const int32_t *sLs = sLc + sRp[nr];
-            for (int r = warp; r < nr; r += kPipeCW) {
+            // a stage whose record does not describe this tile is never used
+            const bool rec_ok = sRp[0] == 0 && sRp[nr] >= 0 && sRp[nr] <= a.maxBlk;
+            if (!rec_ok && lane == 0) atomicExch(a.err, 3);
+            for (int r = rec_ok ? warp : nr; r < nr; r += kPipeCW) {
                 // acc[q] = row q of the block row, columns (c, c+1)
                 float2 acc[4];
 #pragma unroll
@@ -465,15 +521,14 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
                 a.partial[pbase + j * 2 + which] = make_float2(hsum, lsum);
             }
             __syncwarp();
-            if (lane == 0) {
-                mbar_arrive(redfree);
-                // the first reducer hands the tile to the publisher: it has seen every
-                // consumer warp's arrival, so all stores of the tile precede this
-                if (a.flags && rw == 0) {
-                    const int ps = i % kPubSlots;
-                    if (i < kPubSlots ||
-                        wait_phase(&pubfree[ps], (uint32_t)((i / kPubSlots) - 1) & 1u, s_abort, a.err))
-                        mbar_arrive(&pub[ps]);
+            if (lane == 0) mbar_arrive(redfree);
+            // the first reducer hands the tile to the publisher: it has seen every
+            // consumer warp's arrival, so all stores of the tile precede this
+            if (a.flags && rw == 0) {
+                const int ps = i % kPubSlots;
+                if (i < kPubSlots ||
+                    wait_phase(&pubfree[ps], (uint32_t)((i / kPubSlots) - 1) & 1u, s_abort, a.err)) {
+                    if (lane == 0) mbar_arrive(&pub[ps]);
                 }
             }
         }
@@ -589,6 +644,15 @@ int launch_cheb_f32_pipe(cudaStream_t st, const DevMatrix &m, const PipePlan &pl
     a.err = pl.err;
     a.tiles = nullptr;
     a.ntiles = 0;
+    a.flag_spin = kFlagSpin;
+    a.stall_tile = -1;
+    if (multi) {
+        if (const char *v = std::getenv("LARGETB_TEST_WAIT_LIMIT")) {
+            const unsigned long x = std::strtoul(v, nullptr, 10);
+            if (x > 0 && x < kFlagSpin) a.flag_spin = (uint32_t)x;
+        }
+        if (const char *v = std::getenv("LARGETB_TEST_STALL_TILE")) a.stall_tile = (int)std::strtol(v, nullptr, 10);
+    }
     const int ntiles = pl.G * a.nchunk;
     const int grid = std::min(ntiles, pl.nsm);
     const size_t smem = cheb_f32_pipe_smem(pl.stage_bytes, pl.stages);
@@ -627,6 +691,8 @@ void launch_cheb_f32_pipe_batch(cudaStream_t st, const PipePlan &pl, const PipeB
     a.err = pl.err;
     a.tiles = tiles;
     a.ntiles = ntiles;
+    a.flag_spin = kFlagSpin;
+    a.stall_tile = -1;
     const int grid = std::min(ntiles, pl.nsm);
     if (grid < 1) return;
     k_cheb_f32_pipe<true><<<grid, kPipeThreads, cheb_f32_pipe_smem(pl.stage_bytes, pl.stages), st>>>(a);
