@@ -240,6 +240,26 @@ int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, do
  * carries iterations, ||X^2 - X||_F and the stored block count. */
 int tb_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep);
 
+/* The reference's default, stochastic density path (runKPM +
+ * computeDensityMatrix with random vectors): replaces the DOS, chemical
+ * potential and interval refinement of runKPM (withSP2_deltaH.cpp:1579-1703,
+ * random vectors 1236-1264) and computeDiagonalElements' random-vector
+ * estimator (1296-1399).  On H (+ diag(shift) if given, n doubles):
+ *   1. the stochastic KPM DOS of tb_kpm_dos with n_probes Gaussian probes
+ *      (counter-based stream `seed`), dos_moments Jackson-damped moments and
+ *      dos_points nodes on the Gershgorin interval;
+ *   2. mu where the DOS area from the bottom reaches N_e/(2n) of the total,
+ *      and the interval [E_min, E_max] where DOS/n >= 0.001 first holds
+ *      from either end (X = (H - b)/a with a, b of that interval);
+ *   3. diagP_i = sum_r x_i (P x)_i / sum_r x_i^2 over n_probes fresh probes
+ *      (stream seed + 1), P x = sum_{k<M} c_k g_k T_k(X) x with the Fermi
+ *      (kT > 0) or step (kT <= 0) coefficients at mu and tb_params.kernel.
+ * FP64 throughout.  diagP (n, per spin), q (natoms, both spins), mu
+ * (Hartree); the report gives a, b, mu and timings. */
+int tb_density_stochastic(tb_ctx *ctx, const double *shift, int32_t n_probes, uint64_t seed,
+                          int32_t dos_moments, int32_t dos_points, double *diagP, double *q, double *mu,
+                          tb_report *rep);
+
 /* Stochastic KPM density of states of H (runKPM's DOS, withSP2_deltaH.cpp:1579-1648):
  * n_random Gaussian vectors (counter-based splitmix64/Box-Muller with `seed`),
  * n_moments Jackson-damped moments, the DOS at npts Chebyshev nodes.  Writes

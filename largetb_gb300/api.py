@@ -158,6 +158,8 @@ def load(build_if_missing: bool = True):
     L.tb_sp2.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(TbReport)]
     L.tb_kpm_dos.argtypes = [_vp, C.c_int32, C.c_int32, C.c_uint64, C.c_int32, _vp, _vp, _vp,
                              C.POINTER(TbReport)]
+    L.tb_density_stochastic.argtypes = [_vp, _vp, C.c_int32, C.c_uint64, C.c_int32, C.c_int32, _vp, _vp,
+                                        C.POINTER(C.c_double), C.POINTER(TbReport)]
     L.tb_last_error.argtypes = [_vp]
     L.tb_last_error.restype = C.c_char_p
     L.tb_status_string.argtypes = [C.c_int]
@@ -400,6 +402,18 @@ class Context:
         self._check(self._L.tb_sp2(self._h, _ptr(diagP), _ptr(q), C.byref(eb), C.byref(rep)),
                     allow=(TB_ERR_NOT_CONVERGED,))
         return dict(diagP=diagP, q=q, e_band=eb.value, report=rep.as_dict())
+
+    def density_stochastic(self, n_probes=20, seed=0, dos_moments=1000, dos_points=2000, shift=None):
+        """runKPM's stochastic DOS, mu from its area and the refined interval,
+        then computeDiagonalElements' random-vector estimator."""
+        diagP = np.zeros(self.n)
+        q = np.zeros(self.natoms)
+        mu = C.c_double()
+        rep = TbReport()
+        sh = None if shift is None else np.ascontiguousarray(shift, np.float64)
+        self._check(self._L.tb_density_stochastic(self._h, _ptr(sh), n_probes, seed, dos_moments, dos_points,
+                                                  _ptr(diagP), _ptr(q), C.byref(mu), C.byref(rep)))
+        return dict(diagP=diagP, q=q, mu=mu.value, report=rep.as_dict())
 
     def kpm_dos(self, n_moments=1000, n_random=20, seed=0, npts=2000):
         mom = np.zeros(n_moments)

@@ -1745,6 +1745,63 @@ int tb_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *rep
     TB_ABI_CATCH
 }
 
+int tb_density_stochastic(tb_ctx *ctx, const double *shift, int32_t n_probes, uint64_t seed,
+                          int32_t dos_moments, int32_t dos_points, double *diagP, double *q, double *mu,
+                          tb_report *rep)
+{
+    TB_ABI_TRY
+    if (!ctx) return TB_ERR_INVALID_ARG;
+    if (!ctx->have_h) return fail(ctx, TB_ERR_NOT_READY, "Hamiltonian not set");
+    if (!(ctx->p.n_electrons > 0))
+        return fail(ctx, TB_ERR_NOT_READY, "n_electrons unset (give it in tb_params or tb_set_scc)");
+    if (n_probes < 1 || n_probes > 65536 || dos_moments < 2 || dos_moments > 100000 || dos_points < 2 ||
+        dos_points > 1000000)
+        return fail(ctx, TB_ERR_INVALID_ARG,
+                    "need 1 <= n_probes <= 65536, 2 <= dos_moments <= 100000, 2 <= dos_points <= 1e6");
+    if (shift)
+        for (int i = 0; i < ctx->m.n; i++)
+            if (!std::isfinite(shift[i])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in shift");
+    TB_TRY(set_device(ctx));
+    TB_TRY(ensure_work(ctx));
+    cudaEvent_t e0;
+    begin_call(ctx, &e0);
+    if (shift)
+        TB_CUDA(cudaMemcpyAsync(ctx->w.shift, shift, sizeof(double) * ctx->m.n, cudaMemcpyHostToDevice,
+                                ctx->stream));
+    int64_t nl = 0;
+    TB_TRY(run_density_stochastic(ctx, shift ? ctx->w.shift : nullptr, n_probes, seed, dos_moments, dos_points,
+                                  &nl));
+    DevState hs;
+    TB_CUDA(cudaMemcpyAsync(&hs, ctx->w.state, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+    if (diagP) TB_CUDA(cudaMemcpyAsync(diagP, ctx->w.diagP, ctx->m.n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (q) TB_CUDA(cudaMemcpyAsync(q, ctx->w.q, ctx->m.natoms * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (hs.status == TB_ERR_SPECTRUM)
+        return fail(ctx, TB_ERR_SPECTRUM, "DOS support collapsed or too wide for the quadrature");
+    if (mu) *mu = hs.mu;
+    cudaEvent_t e1;
+    cudaEventCreate(&e1);
+    cudaEventRecord(e1, ctx->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rep) {
+        std::memset(rep, 0, sizeof(*rep));
+        rep->lmin = hs.lmin;
+        rep->lmax = hs.lmax;
+        rep->a = hs.a;
+        rep->b = hs.b;
+        rep->mu = hs.mu;
+        rep->t_total_ms = ms;
+        rep->kernel_launches = nl;
+        rep->precision = TB_PREC_FP64;
+    }
+    return TB_OK;
+    TB_ABI_CATCH
+}
+
 int tb_kpm_dos(tb_ctx *ctx, int32_t n_moments, int32_t n_random, uint64_t seed, int32_t npts,
                double *moments, double *energies, double *dos, tb_report *rep)
 {

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "tb_internal.h"
@@ -84,7 +85,213 @@ __global__ void k_dos_eval(const double *__restrict__ g, const double *__restric
     E[q] = x * st->a + st->b;
 }
 
+// Chemical potential and refined spectral interval from the DOS on the
+// nodes (runKPM, withSP2_deltaH.cpp:1663-1703), written into the state for
+// the density pass: trapezoid area from the bottom of the spectrum up to
+// N_e / (2n) of the total gives mu = E[index]; the interval is where
+// DOS/n >= 0.001 first holds from either end (-10, 10 when it never does).
+// One thread: a sequential scan of npts values.  Also sets beta_x = a/kT
+// and the quadrature size of the new interval (the Gershgorin rule).
+__global__ void k_dos_mu(const double *__restrict__ E, const double *__restrict__ dos, int npts, int n,
+                         double n_elec, double kT, int M, int nq_cap, DevState *st)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double dosall = 0.0;
+    for (int i = npts - 1; i > 0; i--) {
+        const double xi = cos(kPi * (i + 0.5) / npts), xm = cos(kPi * (i - 0.5) / npts);
+        dosall += (xm - xi) * (dos[i] + dos[i - 1]) / 2;
+    }
+    const double area = n_elec * dosall / (2.0 * n);
+    double cum = 0.0;
+    int mi = 0;
+    for (int i = npts - 1; i > 0; i--) {
+        const double xi = cos(kPi * (i + 0.5) / npts), xm = cos(kPi * (i - 0.5) / npts);
+        cum += (xm - xi) * (dos[i] + dos[i - 1]) / 2;
+        if (cum >= area) {
+            mi = i;
+            break;
+        }
+    }
+    double emin = -10.0, emax = 10.0;
+    for (int i = npts - 1; i > 0; i--)
+        if (dos[i] / n >= 0.001) {
+            emin = E[i];
+            break;
+        }
+    for (int i = 0; i < npts; i++)
+        if (dos[i] / n >= 0.001) {
+            emax = E[i];
+            break;
+        }
+    const double a = (emax - emin) / 2, b = (emax + emin) / 2;
+    st->a = a;
+    st->b = b;
+    st->mu = E[mi];
+    st->mu_x = (E[mi] - b) / a;
+    st->status = (a > 0 && isfinite(a)) ? 0 : TB_ERR_SPECTRUM;
+    st->beta_x = kT > 0 ? a / kT : 0.0;
+    double need = 4.0 * M;
+    if (st->beta_x > 0 && 13.0 * st->beta_x > need) need = 13.0 * st->beta_x;
+    if (need < 256) need = 256;
+    int nq = 256;
+    while (nq < need && nq < (1 << 22)) nq *= 2;
+    if (nq > nq_cap) st->status = TB_ERR_SPECTRUM;
+    st->nq = nq > nq_cap ? nq_cap : nq;
+    st->bisect_done = 1;
+}
+
+// Probe slab of the density pass: columns t < nr of probes t0 .. t0+nr-1 of
+// the stream `seed` (deviate index (t0 + t) n + i), zero beyond.
+__global__ void k_probe_slab(double *__restrict__ T0, double *__restrict__ R, int n, int B, int nr, int t0,
+                             uint64_t seed)
+{
+    const int64_t tot = (int64_t)n * B;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / B), t = (int)(e % B);
+        const double v = t < nr ? gauss_at(seed, (uint64_t)(t0 + t) * n + i) : 0.0;
+        T0[e] = v;
+        R[e] = v;
+    }
+}
+
+// computeDiagonalElements' accumulation for step k: one warp per orbital i,
+// num_i += c_k g_k sum_t R[i][t] T_k[i][t]; at k = 0 also den_i += sum_t R[i][t]^2.
+__global__ void k_probe_rowacc(const double *__restrict__ R, const double *__restrict__ Tk, int n, int B,
+                               const double *__restrict__ c, const double *__restrict__ g, int k,
+                               double *__restrict__ num, double *__restrict__ den)
+{
+    const int lane = threadIdx.x & 31;
+    const int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (i >= n) return;
+    double s = 0.0, s2 = 0.0;
+    for (int t = lane; t < B; t += 32) {
+        const double r = R[(int64_t)i * B + t];
+        s = fma(r, Tk[(int64_t)i * B + t], s);
+        s2 = fma(r, r, s2);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if (lane == 0) {
+        num[i] += c[k] * g[k] * s;
+        if (k == 0) den[i] += s2;
+    }
+}
+
+// diagP_i = num_i / den_i; q_a = 2 sum over the atom's four orbitals.
+__global__ void k_probe_diag(const double *__restrict__ num, const double *__restrict__ den, int natoms,
+                             double *__restrict__ diagP, double *__restrict__ q)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natoms) return;
+    double s = 0.0;
+    for (int r = 0; r < 4; r++) {
+        const double d = num[4 * a + r] / den[4 * a + r];
+        diagP[4 * a + r] = d;
+        s += d;
+    }
+    q[a] = 2.0 * s;
+}
+
 }  // namespace
+
+int run_density_stochastic(tb_ctx *ctx, const double *d_shift, int nr, uint64_t seed, int nmom_dos, int npts,
+                           int64_t *launches)
+{
+    DevMatrix &m = ctx->m;
+    DevWork &w = ctx->w;
+    cudaStream_t st = ctx->stream;
+    const int M = ctx->p.M;
+    const int Bmax = 256;
+    const int B_dos = ((nr + 63) / 64) * 64;
+    const int B = std::min(B_dos, Bmax);
+    double *T0 = nullptr, *T1 = nullptr, *R = nullptr, *mom = nullptr, *gd = nullptr, *E = nullptr,
+           *dos = nullptr, *num = nullptr, *den = nullptr;
+    int rc = TB_OK;
+    cudaError_t e = cudaSuccess;
+    int64_t nl = 0;
+    const int64_t slab = (int64_t)m.n * std::max(B_dos, B);
+    if ((e = cudaMalloc(&T0, sizeof(double) * slab)) || (e = cudaMalloc(&T1, sizeof(double) * slab)) ||
+        (e = cudaMalloc(&R, sizeof(double) * slab)) || (e = cudaMalloc(&mom, sizeof(double) * nmom_dos)) ||
+        (e = cudaMalloc(&gd, sizeof(double) * nmom_dos)) || (e = cudaMalloc(&E, sizeof(double) * npts)) ||
+        (e = cudaMalloc(&dos, sizeof(double) * npts)) || (e = cudaMalloc(&num, sizeof(double) * m.n)) ||
+        (e = cudaMalloc(&den, sizeof(double) * m.n))) {
+        ctx->err = std::string("cudaMalloc(stochastic density): ") + cudaGetErrorString(e);
+        rc = e == cudaErrorMemoryAllocation ? TB_ERR_OUT_OF_MEMORY : TB_ERR_CUDA;
+    }
+    if (rc == TB_OK && !m.x64 && (e = cudaMalloc(&m.x64, sizeof(double) * 16 * m.nnzb))) {
+        ctx->err = std::string("cudaMalloc(x64): ") + cudaGetErrorString(e);
+        rc = TB_ERR_OUT_OF_MEMORY;
+    }
+    if (rc == TB_OK) {
+        // ---- runKPM: stochastic moments of X on the Gershgorin interval ----
+        std::vector<double> gh(nmom_dos);
+        const double N = nmom_dos, cotv = std::cos(kPi / (N + 1)) / std::sin(kPi / (N + 1));
+        for (int k = 0; k < nmom_dos; k++)
+            gh[k] = ((N - k + 1) * std::cos(kPi * k / (N + 1)) + std::sin(kPi * k / (N + 1)) * cotv) / (N + 1);
+        cudaMemcpyAsync(gd, gh.data(), sizeof(double) * nmom_dos, cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(mom, 0, sizeof(double) * nmom_dos, st);
+        launch_gershgorin(st, m, d_shift, ctx->p.spectral_pad, ctx->p.kT, M, w.nq_cap, w.state, ctx->p.bounds_lo,
+                          ctx->p.bounds_hi);
+        launch_build_x(st, m, d_shift, TB_PREC_FP64, w.state);
+        const int64_t tot = (int64_t)m.n * B_dos;
+        const int blocks = (int)std::min<int64_t>((tot + 255) / 256, 152 * 8);
+        k_probe_init<<<blocks, 256, 0, st>>>(T0, R, m.n, B_dos, nr, seed);
+        k_probe_dot<<<blocks, 256, 0, st>>>(R, T0, tot, mom);
+        nl += 4;
+        for (int kout = 1; kout < nmom_dos; kout++) {
+            const bool odd = kout & 1;
+            double *in = odd ? T0 : T1, *out = odd ? T1 : T0;
+            launch_cheb_step_f64(st, m, in, out, B_dos, m.n, kout == 1, nullptr, kout);
+            k_probe_dot<<<blocks, 256, 0, st>>>(R, out, tot, mom + kout);
+            nl += (kout == 1) ? 3 : 2;
+        }
+        k_dos_eval<<<(npts + 127) / 128, 128, 0, st>>>(gd, mom, nmom_dos, npts, w.state, E, dos);
+        // ---- mu and the refined interval; X on it; the expansion coefficients ----
+        k_dos_mu<<<1, 1, 0, st>>>(E, dos, npts, m.n, ctx->p.n_electrons, ctx->p.kT, M, w.nq_cap, w.state);
+        launch_build_x(st, m, d_shift, TB_PREC_FP64, w.state);
+        launch_fermi_coeffs(st, M, w.state, w.nq_cap, w.costab, w.fq, w.c);
+        nl += 5;
+        // ---- computeDiagonalElements: fresh probes (stream seed + 1), slabs of B ----
+        cudaMemsetAsync(num, 0, sizeof(double) * m.n, st);
+        cudaMemsetAsync(den, 0, sizeof(double) * m.n, st);
+        const int rblocks = (int)((((int64_t)m.n * 32) + 255) / 256);
+        for (int t0 = 0; t0 < nr; t0 += B) {
+            const int nrs = std::min(B, nr - t0);
+            const int64_t ts = (int64_t)m.n * B;
+            k_probe_slab<<<(int)std::min<int64_t>((ts + 255) / 256, 152 * 8), 256, 0, st>>>(T0, R, m.n, B, nrs, t0,
+                                                                                             seed + 1);
+            k_probe_rowacc<<<rblocks, 256, 0, st>>>(R, T0, m.n, B, w.c, w.g, 0, num, den);
+            nl += 2;
+            for (int kout = 1; kout < M; kout++) {
+                const bool odd = kout & 1;
+                double *in = odd ? T0 : T1, *out = odd ? T1 : T0;
+                launch_cheb_step_f64(st, m, in, out, B, m.n, kout == 1, nullptr, kout);
+                k_probe_rowacc<<<rblocks, 256, 0, st>>>(R, out, m.n, B, w.c, w.g, kout, num, den);
+                nl += (kout == 1) ? 3 : 2;
+            }
+        }
+        k_probe_diag<<<(m.natoms + 127) / 128, 128, 0, st>>>(num, den, m.natoms, w.diagP, w.q);
+        nl++;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) {
+            ctx->err = std::string("stochastic density: ") + cudaGetErrorString(e);
+            rc = TB_ERR_CUDA;
+        }
+    }
+    cudaFree(T0);
+    cudaFree(T1);
+    cudaFree(R);
+    cudaFree(mom);
+    cudaFree(gd);
+    cudaFree(E);
+    cudaFree(dos);
+    cudaFree(num);
+    cudaFree(den);
+    if (launches) *launches = nl;
+    return rc;
+}
 
 int run_kpm_dos(tb_ctx *ctx, int nmom, int nr, uint64_t seed, int npts, double *mom_h, double *E_h,
                 double *dos_h, double *a_out, double *b_out, int64_t *launches)

@@ -317,6 +317,8 @@ int run_sp2(tb_ctx *ctx, double *diagP, double *q, double *e_band, tb_report *re
             int32_t *branches_out, int32_t branches_cap);
 
 // ---- tb_dos.cu ----------------------------------------------------------
+int run_density_stochastic(tb_ctx *ctx, const double *d_shift, int nr, uint64_t seed, int nmom_dos, int npts,
+                           int64_t *launches);
 int run_kpm_dos(tb_ctx *ctx, int nmom, int nr, uint64_t seed, int npts, double *mom, double *E,
                 double *dos, double *a_out, double *b_out, int64_t *launches);
 

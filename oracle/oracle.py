@@ -147,6 +147,12 @@ def lib():
         L.orc_kpm_dos.argtypes = [
             C.c_int, i32p, i32p, f64p, C.c_double, C.c_double, C.c_int, C.c_int, C.c_uint64,
             C.c_int, f64p, f64p, f64p]
+        L.orc_density_stochastic.argtypes = [
+            C.c_int, i32p, i32p, f64p, i32p, C.c_int, C.POINTER(OrcKpeParams), C.c_int, C.c_uint64,
+            C.c_int, C.c_int, f64p, f64p, C.POINTER(OrcKpeResult)]
+        L.orc_dos_mu.argtypes = [C.c_int, f64p, f64p, C.c_double, C.c_int, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_dos_mu.restype = None
         L.orc_gauss.argtypes = [C.c_uint64, C.c_uint64]
         L.orc_gauss.restype = C.c_double
     return _lib
@@ -458,6 +464,27 @@ def sp2(m: Model, drop_tol=1e-5, max_iter=40, idem_tol=1e-10, trace_tol=0.0, nth
     return dict(diagP=diagP, q=q, iters=r.iters, idem_err=r.idem_err, trace=r.trace,
                 e_band=r.e_band, nnzb=r.nnzb, lmin=r.lmin, lmax=r.lmax,
                 branches=br[: r.iters], idem_hist=ih[: r.iters + 1], trace_hist=th[: r.iters + 1])
+
+
+def density_stochastic(m: Model, p: OrcKpeParams, n_random=20, seed=0, dos_moments=1000,
+                       dos_points=2000):
+    """runKPM (stochastic DOS, mu from its area, refined a, b) +
+    computeDensityMatrix's ratio estimator (see tb_oracle.h)."""
+    diagP = np.zeros(m.n)
+    q = np.zeros(m.natoms)
+    res = OrcKpeResult()
+    _check(lib().orc_density_stochastic(m.n, m.rowptr, m.col, m.val, m.orb2atom, m.natoms, C.byref(p),
+                                        n_random, seed, dos_moments, dos_points, diagP, q,
+                                        C.byref(res)), "density_stochastic")
+    return dict(diagP=diagP, q=q, mu=res.mu, mu_x=res.mu_x, a=res.a, b=res.b, lmin=res.lmin,
+                lmax=res.lmax)
+
+
+def dos_mu(energies, dos, n_elec, n):
+    mu, mi, a, b = C.c_double(), C.c_int(), C.c_double(), C.c_double()
+    lib().orc_dos_mu(len(dos), np.ascontiguousarray(energies, np.float64), np.ascontiguousarray(dos, np.float64),
+                     n_elec, n, C.byref(mu), C.byref(mi), C.byref(a), C.byref(b))
+    return dict(mu=mu.value, mu_index=mi.value, a=a.value, b=b.value)
 
 
 def kpm_dos(m: Model, a, b, nmom=1000, n_random=20, seed=0, npts=2000):

@@ -1274,3 +1274,150 @@ int orc_kpm_dos(int n, const int32_t *rowptr, const int32_t *col, const double *
     free(v1);
     return ORC_OK;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Stochastic-trace density                                                  */
+/* ------------------------------------------------------------------------- */
+void orc_dos_mu(int npts, const double *energies, const double *dos, double n_elec, int n,
+                double *mu, int *mu_index, double *a, double *b)
+{
+    /* node abscissae as runKPM has them: x_k = cos(pi (k+1/2)/npts), falling in k */
+    double dosall = 0.0;
+    for (int i = npts - 1; i > 0; i--) {
+        const double xi = cos(ORC_PI * (i + 0.5) / npts), xm = cos(ORC_PI * (i - 0.5) / npts);
+        dosall += (xm - xi) * (dos[i] + dos[i - 1]) / 2;
+    }
+    const double area = n_elec * dosall / (2.0 * n);
+    double cum = 0.0;
+    int mi = 0;
+    for (int i = npts - 1; i > 0; i--) {
+        const double xi = cos(ORC_PI * (i + 0.5) / npts), xm = cos(ORC_PI * (i - 0.5) / npts);
+        cum += (xm - xi) * (dos[i] + dos[i - 1]) / 2;
+        if (cum >= area) {
+            mi = i;
+            break;
+        }
+    }
+    double emin = -10.0, emax = 10.0;
+    for (int i = npts - 1; i > 0; i--)
+        if (dos[i] / n >= 0.001) {
+            emin = energies[i];
+            break;
+        }
+    for (int i = 0; i < npts; i++)
+        if (dos[i] / n >= 0.001) {
+            emax = energies[i];
+            break;
+        }
+    *mu = energies[mi];
+    *mu_index = mi;
+    *a = (emax - emin) / 2;
+    *b = (emax + emin) / 2;
+}
+
+int orc_density_stochastic(int n, const int32_t *rowptr, const int32_t *col, const double *val,
+                           const int32_t *orb2atom, int natoms, const orc_kpe_params *p,
+                           int n_random, uint64_t seed, int dos_moments, int dos_points,
+                           double *diagP, double *q, orc_kpe_result *res)
+{
+    const int M = p->M;
+    if (M < 2 || n < 1 || n_random < 1 || dos_moments < 2 || dos_points < 2) return ORC_ERR_ARG;
+    orc_kpe_result r;
+    memset(&r, 0, sizeof(r));
+    orc_gershgorin(n, rowptr, col, val, NULL, &r.lmin, &r.lmax);
+    const double a0 = 0.5 * (r.lmax - r.lmin) * (1.0 + p->pad), b0 = 0.5 * (r.lmax + r.lmin);
+    if (!(a0 > 0)) return ORC_ERR_ARG;
+    double *mom = (double *)malloc(sizeof(double) * dos_moments);
+    double *E = (double *)malloc(sizeof(double) * dos_points);
+    double *dos = (double *)malloc(sizeof(double) * dos_points);
+    int err = orc_kpm_dos(n, rowptr, col, val, a0, b0, dos_moments, n_random, seed, dos_points, mom, E, dos);
+    if (err) {
+        free(mom);
+        free(E);
+        free(dos);
+        return err;
+    }
+    int mi = 0;
+    orc_dos_mu(dos_points, E, dos, p->n_elec, n, &r.mu, &mi, &r.a, &r.b);
+    free(mom);
+    free(E);
+    free(dos);
+    if (!(r.a > 0)) return ORC_ERR_ARG;
+    r.mu_x = (r.mu - r.b) / r.a;
+    double *g = (double *)malloc(sizeof(double) * M);
+    if (p->kernel == 0)
+        orc_jackson(M, g);
+    else if (p->kernel == 1)
+        orc_kernel_autocorr(M, g);
+    else
+        for (int k = 0; k < M; k++) g[k] = 1.0;
+    g[0] = 1.0;
+    double *c = (double *)malloc(sizeof(double) * M);
+    const double beta_x = p->kT > 0 ? r.a / p->kT : 0.0;
+    if (beta_x > 0)
+        orc_fermi_coeffs(M, r.mu_x, beta_x, orc_quadrature_nodes(M, beta_x), c);
+    else
+        orc_step_coeffs(M, r.mu_x, c);
+    /* X = (H - b)/a */
+    double *xv = (double *)malloc(sizeof(double) * (rowptr[n] > 0 ? rowptr[n] : 1));
+    double *xd = (double *)malloc(sizeof(double) * n);
+    for (int i = 0; i < n; i++) {
+        int found = 0;
+        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+            if (col[k] == i) {
+                xv[k] = (val[k] - r.b) / r.a;
+                found = 1;
+            } else
+                xv[k] = val[k] / r.a;
+        }
+        xd[i] = found ? 0.0 : -r.b / r.a;
+    }
+    double *x = (double *)malloc(sizeof(double) * n);
+    double *v0 = (double *)malloc(sizeof(double) * n);
+    double *v1 = (double *)malloc(sizeof(double) * n);
+    double *num = (double *)calloc(n, sizeof(double));
+    double *den = (double *)calloc(n, sizeof(double));
+    for (int t = 0; t < n_random; t++) {
+        for (int i = 0; i < n; i++) {
+            x[i] = orc_gauss(seed + 1, (uint64_t)t * n + i);
+            v0[i] = x[i];
+            den[i] += x[i] * x[i];
+            num[i] += c[0] * g[0] * x[i] * x[i];
+        }
+        for (int i = 0; i < n; i++) {
+            double acc = xd[i] * v0[i];
+            for (int k = rowptr[i]; k < rowptr[i + 1]; k++) acc += xv[k] * v0[col[k]];
+            v1[i] = acc;
+            num[i] += c[1] * g[1] * x[i] * acc;
+        }
+        for (int kk = 2; kk < M; kk++) {
+            for (int i = 0; i < n; i++) {
+                double acc = xd[i] * v1[i];
+                for (int k = rowptr[i]; k < rowptr[i + 1]; k++) acc += xv[k] * v1[col[k]];
+                v0[i] = 2.0 * acc - v0[i];
+            }
+            for (int i = 0; i < n; i++) num[i] += c[kk] * g[kk] * x[i] * v0[i];
+            double *tmp = v0;
+            v0 = v1;
+            v1 = tmp;
+        }
+    }
+    if (q)
+        for (int at = 0; at < natoms; at++) q[at] = 0.0;
+    for (int i = 0; i < n; i++) {
+        const double d = num[i] / den[i];
+        if (diagP) diagP[i] = d;
+        if (q) q[orb2atom[i]] += 2.0 * d;
+    }
+    if (res) *res = r;
+    free(g);
+    free(c);
+    free(xv);
+    free(xd);
+    free(x);
+    free(v0);
+    free(v1);
+    free(num);
+    free(den);
+    return ORC_OK;
+}

@@ -250,6 +250,31 @@ int orc_kpm_dos(int n, const int32_t *rowptr, const int32_t *col, const double *
                 double b, int nmom, int n_random, uint64_t seed, int npts, double *mom,
                 double *energies, double *dos);
 
+/* Chemical potential and refined spectral interval from a DOS on the npts
+ * Chebyshev nodes x_k = cos(pi (k+1/2)/npts) (energies E_k = a0 x_k + b0):
+ * restates runKPM, withSP2_deltaH.cpp:1663-1703.  The trapezoid area from
+ * the bottom of the spectrum reaches N_e/(2n) of the total at node mu_index,
+ * mu = E[mu_index]; the interval [E_min, E_max] is where DOS/n >= 0.001 first
+ * holds from either end (-10, 10 when it never does); a = (E_max - E_min)/2,
+ * b = (E_max + E_min)/2. */
+void orc_dos_mu(int npts, const double *energies, const double *dos, double n_elec, int n,
+                double *mu, int *mu_index, double *a, double *b);
+
+/* Stochastic-trace density, the reference's default path: runKPM's DOS from
+ * n_random Gaussian probes (seed) with dos_moments Jackson-damped moments on
+ * dos_points nodes, mu and the refined interval from it (orc_dos_mu), then
+ * computeDiagonalElements' ratio estimator (withSP2_deltaH.cpp:1296-1399)
+ *   diagP_i = sum_r x_i^r (P x^r)_i / sum_r (x_i^r)^2,
+ *   P x = sum_{k<M} c_k g_k T_k(X) x  (getKPE, withSP2_deltaH.cpp:1134-1168)
+ * on X = (H - b)/a with n_random fresh probes (stream seed + 1), c_k the
+ * Fermi (kT > 0) or step (kT <= 0) coefficients at mu_x = (mu - b)/a and g_k
+ * p->kernel's damping.  q_a = 2 sum_{i in a} diagP_i.  res receives a, b,
+ * mu, mu_x and the Gershgorin bounds. */
+int orc_density_stochastic(int n, const int32_t *rowptr, const int32_t *col, const double *val,
+                           const int32_t *orb2atom, int natoms, const orc_kpe_params *p,
+                           int n_random, uint64_t seed, int dos_moments, int dos_points,
+                           double *diagP, double *q, orc_kpe_result *res);
+
 /* Counter-based N(0,1) deviate: Box-Muller (cosine branch) on outputs 2*index
  * and 2*index+1 of the splitmix64 stream seeded with `seed`.  The CUDA path
  * and the product's model builder use the same definition. */
