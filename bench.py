@@ -38,7 +38,9 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(workload="beta-cristobalite 6x6x6 SCC solve", cells=[6, 6, 6], atoms=5184,
                 orbitals=20736, sigma_ang=0.05, seed=2002, M=400, kT=0.01, scc_tol=1e-6,
                 cutoff_bohr=4.0, mixer="anderson(16, 0.2); 0.1 from the learned start",
-                trace="exact, all identity columns")
+                trace="exact, all identity columns",
+                l2="GPU arm: a 256 MB buffer is written between timed steps (L2 flush)",
+                parallelism="replicas (one independent solve per GPU)")
 METRIC = "s per converged SCC solve (5184 atoms, |dq|<1e-6 e)"
 
 
@@ -147,28 +149,58 @@ def l2_flush(device):
     torch.cuda.synchronize(device)
 
 
-def cpu_sample(model_o, M, n_threads, iters):
-    """FP64 oracle exact-trace moments on a bounded sample of identity columns
-    and Chebyshev steps, scaled to one converged solve."""
+def oracle_fixture(cells):
+    """The FP64-oracle SCC of this cell, run to convergence on the CPU and
+    committed as a fixture (tests/golden/make_scc_oracle.py), or None."""
+    path = os.path.join(ROOT, "tests", "golden", "scc_oracle_%dx%dx%d.npz" % tuple(cells))
+    return np.load(path) if os.path.exists(path) else None
+
+
+def scc_iterations(cells):
+    """SCC iterations of the FP64 oracle to |dq| < 1e-6 e on this cell (the
+    committed fixture), or None when the cell has no fixture."""
+    fx = oracle_fixture(cells)
+    return None if fx is None else int(fx["iters"])
+
+
+def cpu_sample(model_o, M, n_threads, iters, iters_src, cols=None):
+    """FP64 oracle on a bounded sample of the workload, timed: the complete
+    Chebyshev recurrence (all M + 1 moments) of a contiguous block of
+    identity columns.  Every column costs the same (same matrix, same
+    steps), so columns scale it exactly to one density evaluation; the
+    oracle's own SCC iteration count on this cell scales that to a solve."""
     from oracle import oracle as O
     lo, hi = O.gershgorin(model_o)
     a, b = (hi - lo) / 2, (hi + lo) / 2
-    cols = 32 * n_threads
-    steps = 100
+    cols = min(model_o.n, cols or 256 * n_threads)
     t0 = time.perf_counter()
-    O.exact_moments_cols(model_o, a, b, steps + 1, 0, cols, nthreads=n_threads)
+    O.exact_moments_cols(model_o, a, b, M + 1, 0, cols, nthreads=n_threads)
     dt = time.perf_counter() - t0
-    per_eval = dt * (model_o.n / cols) * ((M + 1) / (steps + 1))
+    per_eval = dt * (model_o.n / cols)
     return dict(value=per_eval * iters, unit="s", cores=n_threads, kind="port",
-                sample=(f"FP64 oracle moments of {cols} of {model_o.n} identity columns x {steps} of "
-                        f"{M} Chebyshev steps in {dt:.1f} s, scaled by columns and steps to one "
-                        f"density evaluation ({per_eval:.1f} s) x {iters} SCC iterations"))
+                sample=(f"FP64 oracle, complete {M}-step recurrences of {cols} of {model_o.n} identity "
+                        f"columns in {dt:.2f} s on {n_threads} threads, x {model_o.n / cols:.2f} columns = "
+                        f"{per_eval:.1f} s per density evaluation, x {iters} SCC iterations ({iters_src})"))
+
+
+def measured_oracle_solve(cells):
+    """The one full FP64-oracle SCC solve of this cell that was run end to
+    end (to build the fixture): its wall time, iterations and threads."""
+    fx = oracle_fixture(cells)
+    if fx is None:
+        return None
+    it = int(fx["iters"])
+    return {"s": float(np.sum(fx["eval_s"][:it])), "iters": it, "threads": int(fx["threads"]),
+            "host": "the x86-64 development container that generated the fixture"}
 
 
 def run_reference(args, ws, rank):
     """The reference arm: the reference's own CPU code cannot be built here
-    (PETSc/MPI absent), so its FP64 restatement (oracle/) runs on all host
-    threads over a bounded sample of the same workload."""
+    (PETSc and MPI are external libraries absent from this image), so its
+    FP64 restatement (oracle/) runs on all host threads.  Each step times a
+    bounded sample of the workload (complete recurrences of a block of
+    identity columns) scaled to a solve with the oracle's own iteration
+    count on this cell."""
     if rank != 0:
         return
     from oracle import oracle as O
@@ -176,23 +208,29 @@ def run_reference(args, ws, rank):
     c = WORKLOAD["cells"]
     mo = O.cristobalite(*c, sigma_ang=WORKLOAD["sigma_ang"], seed=WORKLOAD["seed"])
     nth = os.cpu_count() or 1
-    # SCC iteration count of the oracle on the 2x2x2 cell with the same M, kT, mixer
-    small = O.cristobalite(2, 2, 2, sigma_ang=WORKLOAD["sigma_ang"], seed=WORKLOAD["seed"])
-    r = O.scc(small, O.kpe_params(M=WORKLOAD["M"], kT=WORKLOAD["kT"], n_elec=small.n_elec,
-                                  nthreads=nth), tol=1e-6, max_iter=100, beta=0.2, history=16)
+    iters = scc_iterations(c)
+    src = "the FP64 oracle's converged SCC of this cell, committed fixture"
+    if iters is None:  # no fixture for this cell: the oracle's own SCC on the 2x2x2 cell
+        small = O.cristobalite(2, 2, 2, sigma_ang=WORKLOAD["sigma_ang"], seed=WORKLOAD["seed"])
+        iters = O.scc(small, O.kpe_params(M=WORKLOAD["M"], kT=WORKLOAD["kT"], n_elec=small.n_elec,
+                                         nthreads=nth), tol=1e-6, max_iter=100, beta=0.2, history=16)["iters"]
+        src = "the FP64 oracle's SCC on the 2x2x2 cell"
     vals = []
     for i in range(args.warmup + args.steps):
-        cb = cpu_sample(mo, WORKLOAD["M"], nth, r["iters"])
+        # warm-up steps take a quarter of the sample; each timed step ~3 s on 16 cores
+        cb = cpu_sample(mo, WORKLOAD["M"], nth, iters, src, cols=(16 if i < args.warmup else 64) * nth)
         if i >= args.warmup:
             vals.append(cb["value"])
     v = statistics.mean(vals)
     cb["value"] = v
     cb["kind"] = "port"
-    cb["sample"] += " (iterations from the oracle's own SCC on the 2x2x2 cell)"
+    cb["sample"] += f"; mean of {args.steps} timed samples"
+    full = measured_oracle_solve(c)
     line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": dict(WORKLOAD), "impl": "reference", "cpu_baseline": cb,
+            "oracle_full_solve_measured": full,
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -246,8 +284,7 @@ def run_batch_bench(args, T, dev, rank):
     if not args.no_plain:  # the single-structure loops beside the batch
         loop32, t32 = loop(T.PREC_FP32, range(len(models)))
         loop64, t64 = loop(T.PREC_FP64, sub)
-    if rank == 0:
-        print(json.dumps({
+    out = {
             "metric": f"atoms*moments/s, batched SCC of {len(models)} uneven cristobalite cells (M = 300)",
             "value": statistics.mean(am), "unit": "atom-moments/s", "higher_is_better": True,
             "s_per_batch_solve": statistics.mean(ts), "structures": len(models),
@@ -261,7 +298,10 @@ def run_batch_bench(args, T, dev, rank):
             "speedup_vs_loop_plain_fp64": statistics.mean(am) / loop64 if loop64 else None,
             "speedup_vs_loop_fp32": statistics.mean(am) / loop32 if loop32 else None,
             "config": {"dims": [d for d, _, _ in ms], "sigma_ang": [round(sg, 4) for _, sg, _ in ms],
-                       "seed": 4004, "M": M, "kT": 0.01, "scc_tol": 1e-6}}), flush=True)
+                       "seed": 4004, "M": M, "kT": 0.01, "scc_tol": 1e-6}}
+    if rank == 0 and args.batch:
+        print(json.dumps(out), flush=True)
+    return out
 
 
 def run_learned_eval(args, T, dev, rank):
@@ -285,9 +325,8 @@ def run_learned_eval(args, T, dev, rank):
     c.set_params(mix_beta=learned.MIX_BETA)
     rl = c.scc_solve(q_init=q_init)
     c.close()
-    if rank == 0:
-        tz, tl = rz["report"]["t_total_ms"] / 1e3, rl["report"]["t_total_ms"] / 1e3 + t_mlp
-        print(json.dumps({"metric": "SCC iterations and s to |dq|<1e-6 e, 8x8x8 cristobalite",
+    tz, tl = rz["report"]["t_total_ms"] / 1e3, rl["report"]["t_total_ms"] / 1e3 + t_mlp
+    out = {"metric": "SCC iterations and s to |dq|<1e-6 e, 8x8x8 cristobalite",
                           "config": {"cells": cells, "atoms": m.natoms, "orbitals": m.n, "sigma_ang": 0.08,
                                      "seed": 8008, "M": 200, "precision": "fp32"},
                           "zero_start": {"iters": rz["iters"], "s": tz},
@@ -295,7 +334,10 @@ def run_learned_eval(args, T, dev, rank):
                                             "start_err_max_e": float(np.abs(q_init - rz["q"]).max()),
                                             "q0_err_max_e": float(np.abs(m.q0 - rz["q"]).max())},
                           "speedup": tz / tl,
-                          "max_dq_between_solutions": float(np.abs(rz["q"] - rl["q"]).max())}), flush=True)
+                          "max_dq_between_solutions": float(np.abs(rz["q"] - rl["q"]).max())}
+    if rank == 0 and args.learned_eval:
+        print(json.dumps(out), flush=True)
+    return out
 
 
 def run_sp2_bench(args, T, dev, rank):
@@ -334,12 +376,14 @@ def run_sp2_bench(args, T, dev, rank):
                 "max_dq": float(np.abs(out[name + "_q"] - ex["q"]).max()),
                 "e_band_per_atom": abs(out[name]["e_band"] - float(ex["e_band"])) / m.natoms}
     dq = float(np.abs(out.pop("fp32_q") - out.pop("fp64_q")).max())
-    if rank == 0:
-        print(json.dumps({"metric": "s per SP2 purification (1536 atoms, drop 1e-5)",
+    res = {"metric": "s per SP2 purification (1536 atoms, drop 1e-5)",
                           "config": {"cells": cells, "atoms": m.natoms, "sigma_ang": 0.08,
                                      "seed": 3003, "drop_tol": 1e-5, "max_iter": 40},
                           "fp32": out["fp32"], "fp64": out["fp64"],
-                          "max_dq_fp32_vs_fp64": dq}), flush=True)
+                          "max_dq_fp32_vs_fp64": dq}
+    if rank == 0 and args.sp2:
+        print(json.dumps(res), flush=True)
+    return res
 
 
 def run_all_kernels(T, dev):
@@ -399,6 +443,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 solve (with --batch: the single-structure loops)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the SP2, batch and learned-start figures added to the headline line")
     ap.add_argument("--column-block", type=int, default=0)
     ap.add_argument("--fp32-kernel", type=int, default=0,
                     help="0 autotune, 1 staged, 2 persistent, 3 pipelined (one launch per slab), "
@@ -546,9 +592,9 @@ def main():
         "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 recurrence, f64 moments",
         "data": "synthetic (seeded beta-cristobalite)",
-        "config": dict(cfg, column_block=B, precision="fp32",
-                       l2="64 Mi-float (256 MB) buffer written between timed steps",
-                       parallelism=f"replicas x{ws}"),
+        "config": cfg,
+        "impl_config": {"column_block": B, "precision": "fp32 recurrence, fp64 moments",
+                        "replicas": ws},
         "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
@@ -572,6 +618,7 @@ def main():
         l2_flush(dev)
         r64 = ctx64.scc_solve()
         rep64 = r64["report"]
+        q64, eb64 = r64["q"], r64["e_band"]
         line["plain_fp64"] = {"s_per_solve": rep64["t_total_ms"] / 1e3, "iters": r64["iters"],
                               "start": "neutral q0",
                               "moments_s": rep64["t_moments_ms"] / 1e3,
@@ -584,13 +631,40 @@ def main():
         line["plain_fp64"]["same_H"] = {"max_dq": float(np.abs(d32["q"] - d64["q"]).max()),
                                         "e_band_diff_per_atom": abs(d32["e_band"] - d64["e_band"]) / m.natoms}
         ctx64.close()
+    fx = oracle_fixture(cells)
+    if fx is not None:
+        # against the FP64 oracle's converged SCC of the same cell (fixture)
+        line["vs_fp64_oracle"] = {
+            "oracle_iters": int(fx["iters"]),
+            "fast_max_dq": float(np.abs(q32 - fx["q"]).max()),
+            "fast_max_dq_vs_fixed_point": float(np.abs(q32 - fx["q_tight"]).max()),
+            "fast_e_band_per_atom": abs(eb32 - float(fx["e_band"])) / m.natoms}
+        if "plain_fp64" in line:
+            line["vs_fp64_oracle"].update({
+                "plain_iters": line["plain_fp64"]["iters"],
+                "plain_max_dq": float(np.abs(q64 - fx["q"]).max()),
+                "plain_e_band_per_atom": abs(eb64 - float(fx["e_band"])) / m.natoms})
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         O.build()
         mo = O.cristobalite(*cells, sigma_ang=cfg["sigma_ang"], seed=cfg["seed"])
-        it = line.get("plain_fp64", {}).get("iters", iters[-1])
-        line["cpu_baseline"] = cpu_sample(mo, M, os.cpu_count() or 1, it)
+        it = scc_iterations(cells)
+        src = "the FP64 oracle's converged SCC of this cell, committed fixture"
+        if it is None:
+            it = line.get("plain_fp64", {}).get("iters", iters[-1])
+            src = "the plain FP64 GPU solve of this cell"
+        line["cpu_baseline"] = cpu_sample(mo, M, os.cpu_count() or 1, it, src)
+        line["oracle_full_solve_measured"] = measured_oracle_solve(cells)
     ctx.close()
+    if not args.no_extras and list(cells) == WORKLOAD["cells"]:
+        # the other configurations, measured on the same box after the timed
+        # region (outside it): SP2 purification, the 64-cell batch, the
+        # learned start on 8x8x8
+        sub = argparse.Namespace(**vars(args))
+        sub.cells, sub.steps, sub.warmup, sub.no_plain = None, 1, 1, True
+        line["sp2_4x4x4"] = run_sp2_bench(sub, T, dev, rank)
+        line["batch_64_cells"] = run_batch_bench(sub, T, dev, rank)
+        line["learned_start_8x8x8"] = run_learned_eval(sub, T, dev, rank)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -124,7 +124,14 @@ typedef struct tb_params {
     int32_t no_graphs;     /* 1: launch every kernel of an SCC iteration directly instead of
                               replaying the iteration's captured CUDA graph (debugging,
                               profiling) */
-    int32_t reserved_i;
+    int32_t fp64_small;    /* FP32 form: structures of at most this many orbitals run the plain
+                              FP64 recurrence instead (tb_density, tb_scc_solve, and batch
+                              members, which then leave the batch).  Small structures are
+                              launch-bound, so FP64 costs about what FP32 does there, and it
+                              removes the FP32 recurrence's ~2e-7 e charge noise, which the
+                              SCC response of surface slabs amplifies to ~1e-6 e at the fixed
+                              point.  0: 512 orbitals; -1: never; k > 0: n <= k.
+                              tb_report.fp64_evals counts the evaluations run so. */
     double reserved[2];
 } tb_params;
 
@@ -156,7 +163,9 @@ typedef struct tb_report {
     double fp32_check_ms;     /* CUDA-event time of that check */
     double sp2_flops_done;    /* SP2: 128 x block products actually formed (the symmetric
                                  product forms the blocks J >= I only) */
-    double reserved[3];
+    int32_t fp64_evals;       /* FP32 form: density evaluations run in FP64 by tb_params.fp64_small */
+    int32_t reserved_i;
+    double reserved[2];
 } tb_report;
 
 typedef struct tb_ctx tb_ctx;

@@ -75,7 +75,7 @@ class TbParams(C.Structure):
         ("mode", C.c_int32),
         ("check_fp32", C.c_int32),
         ("no_graphs", C.c_int32),
-        ("reserved_i", C.c_int32),
+        ("fp64_small", C.c_int32),
         ("reserved", C.c_double * 2),
     ]
 
@@ -109,7 +109,9 @@ class TbReport(C.Structure):
         ("fp32_diag_err", C.c_double),
         ("fp32_check_ms", C.c_double),
         ("sp2_flops_done", C.c_double),
-        ("reserved", C.c_double * 3),
+        ("fp64_evals", C.c_int32),
+        ("reserved_i", C.c_int32),
+        ("reserved", C.c_double * 2),
     ]
 
     def as_dict(self):

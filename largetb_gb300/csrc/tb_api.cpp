@@ -1291,6 +1291,113 @@ int host_check_gamma(int32_t natoms, const int32_t *g_rowptr, const int32_t *g_c
 // ===========================================================================
 // C-ABI
 // ===========================================================================
+// The SCC iterations from the state already on the device (ctx->s.qin, the
+// Anderson ring and its meta): the Coulomb shift of the input charges, then
+// one density evaluation and mixing update per iteration until the residual
+// is below scc_tol.  Returns TB_OK, TB_ERR_NOT_CONVERGED at the cap, a state
+// error, or a failure of the launches; *it_out is the last iteration run.
+static int scc_loop(tb_ctx *ctx, int *it_out, DevState &hs)
+{
+    cudaStream_t st = ctx->stream;
+    DevScc &s = ctx->s;
+    DevWork &w = ctx->w;
+    TB_CUDA(cudaMemsetAsync(w.state, 0, sizeof(DevState), st));
+    launch_coulomb_shift(st, s, s.qin, s.V, w.shift);
+    ctx->launches++;
+    std::memset(&hs, 0, sizeof(hs));
+    int it = 0, rc = TB_ERR_NOT_CONVERGED;
+    for (it = 1; it <= ctx->p.scc_max_iter; it++) {
+        bool graphed = false;
+        TB_TRY(scc_iteration(ctx, &graphed));
+        TB_CUDA(cudaGetLastError());
+        TB_TRY(read_state(ctx, hs));
+        if (graphed) {  // the replay's moment phase, timed by the graph's own events
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ctx->graph_ev[0], ctx->graph_ev[1]) == cudaSuccess)
+                ctx->extra_moment_ms += ms;
+            else
+                cudaGetLastError();  // a timing gap is not an error of the solve
+        }
+        if (hs.status) {
+            rc = state_status(ctx, hs);
+            break;
+        }
+        if (hs.converged) {
+            rc = TB_OK;
+            break;
+        }
+    }
+    if (it > ctx->p.scc_max_iter) {
+        it = ctx->p.scc_max_iter;
+        fail(ctx, TB_ERR_NOT_CONVERGED, "SCC reached scc_max_iter");
+    }
+    *it_out = it;
+    return rc;
+}
+
+// tb_params.fp64_small: while alive, a small structure of an FP32 context
+// runs the plain FP64 recurrence (the context's own parameters are restored
+// on destruction).
+struct SmallFp64 {
+    tb_ctx *ctx;
+    bool on = false;
+    int prec = 0, B = 0;
+    explicit SmallFp64(tb_ctx *c) : ctx(c)
+    {
+        const int lim = c->p.fp64_small == 0 ? kSmallFp64N : c->p.fp64_small;
+        if (c->p.precision == TB_PREC_FP32 && lim > 0 && c->m.n <= lim) {
+            on = true;
+            prec = c->p.precision;
+            B = c->p.column_block;
+            c->p.precision = TB_PREC_FP64;
+            c->p.column_block = 256;  // ensure_work trims it to the matrix
+        }
+    }
+    ~SmallFp64()
+    {
+        if (on) {
+            ctx->p.precision = prec;
+            ctx->p.column_block = B;
+        }
+    }
+};
+
+namespace tb {
+
+// The Hamiltonian of a context from an already validated host BSR.
+int set_hamiltonian_bsr(tb_ctx *ctx, int32_t n, int32_t natoms, const HostBsr &hb)
+{
+    ctx->gen++;
+    TB_TRY(set_device(ctx));
+    free_all(ctx);
+    ctx->have_h = ctx->have_scc = false;
+    reset_tuning(ctx);
+    DevMatrix &m = ctx->m;
+    m.n = n;
+    m.natoms = natoms;
+    m.nb = natoms;
+    m.nnzb = (int64_t)hb.bcol.size();
+    TB_TRY(upload(ctx, m.rowptr, hb.brow.data(), hb.brow.size()));
+    TB_TRY(upload(ctx, m.colidx, hb.bcol.data(), hb.bcol.size()));
+    TB_TRY(upload(ctx, m.blkrow, hb.blkrow.data(), hb.blkrow.size()));
+    TB_TRY(upload(ctx, m.diagblk, hb.diagblk.data(), hb.diagblk.size()));
+    TB_TRY(upload(ctx, m.h0, hb.blk.data(), hb.blk.size()));
+    TB_TRY(upload(ctx, m.h0diag, hb.h0diag.data(), hb.h0diag.size()));
+    TB_TRY(upload(ctx, m.radius, hb.radius.data(), hb.radius.size()));
+    TB_TRY(dalloc(ctx, m.xdiag32, (size_t)n));
+    TB_TRY(build_stage_plan(ctx, hb.brow, hb.bcol));
+    TB_TRY(build_persist_plan(ctx, hb.brow, hb.bcol));
+    TB_TRY(build_pipe_plan(ctx, hb.brow, hb.bcol));
+    ctx->h0_lmin = hb.lmin;
+    ctx->h0_lmax = hb.lmax;
+    TB_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->asym_max = hb.asym;
+    ctx->have_h = true;
+    return TB_OK;
+}
+
+}  // namespace tb
+
 extern "C" {
 
 int tb_abi_version(void) { return TB_ABI_VERSION; }
@@ -1429,32 +1536,7 @@ int tb_set_hamiltonian(tb_ctx *ctx, int32_t n, const int32_t *rowptr, const int3
     HostBsr hb;
     const int vrc = host_csr_to_bsr(n, rowptr, colidx, vals, orb2atom, natoms, hb, ctx->err);
     if (vrc) return vrc;
-    TB_TRY(set_device(ctx));
-    free_all(ctx);
-    ctx->have_h = ctx->have_scc = false;
-    reset_tuning(ctx);
-    DevMatrix &m = ctx->m;
-    m.n = n;
-    m.natoms = natoms;
-    m.nb = natoms;
-    m.nnzb = (int64_t)hb.bcol.size();
-    TB_TRY(upload(ctx, m.rowptr, hb.brow.data(), hb.brow.size()));
-    TB_TRY(upload(ctx, m.colidx, hb.bcol.data(), hb.bcol.size()));
-    TB_TRY(upload(ctx, m.blkrow, hb.blkrow.data(), hb.blkrow.size()));
-    TB_TRY(upload(ctx, m.diagblk, hb.diagblk.data(), hb.diagblk.size()));
-    TB_TRY(upload(ctx, m.h0, hb.blk.data(), hb.blk.size()));
-    TB_TRY(upload(ctx, m.h0diag, hb.h0diag.data(), hb.h0diag.size()));
-    TB_TRY(upload(ctx, m.radius, hb.radius.data(), hb.radius.size()));
-    TB_TRY(dalloc(ctx, m.xdiag32, (size_t)n));
-    TB_TRY(build_stage_plan(ctx, hb.brow, hb.bcol));
-    TB_TRY(build_persist_plan(ctx, hb.brow, hb.bcol));
-    TB_TRY(build_pipe_plan(ctx, hb.brow, hb.bcol));
-    ctx->h0_lmin = hb.lmin;
-    ctx->h0_lmax = hb.lmax;
-    TB_CUDA(cudaStreamSynchronize(ctx->stream));
-    ctx->asym_max = hb.asym;
-    ctx->have_h = true;
-    return TB_OK;
+    return set_hamiltonian_bsr(ctx, n, natoms, hb);
     TB_ABI_CATCH
 }
 
@@ -1599,6 +1681,7 @@ int tb_density(tb_ctx *ctx, const double *shift, double *diagP, double *q, doubl
         return tb_sp2(ctx, diagP, q, e_band, rep);
     }
     TB_TRY(set_device(ctx));
+    SmallFp64 small(ctx);
     TB_TRY(ensure_work(ctx));
     cudaEvent_t e0;
     begin_call(ctx, &e0);
@@ -1629,6 +1712,10 @@ int tb_density(tb_ctx *ctx, const double *shift, double *diagP, double *q, doubl
     if (rep) {
         rep->fp32_diag_err = chk_err;
         rep->fp32_check_ms = chk_ms;
+        if (small.on) {
+            rep->fp64_evals = 1;
+            rep->precision = TB_PREC_FP64;
+        }
     }
     return rc;
     TB_ABI_CATCH
@@ -1664,6 +1751,7 @@ int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, do
         for (size_t a = 0; a < na; a++)
             if (!std::isfinite(q_init[a])) return fail(ctx, TB_ERR_NONFINITE, "NaN/Inf in q_init");
     TB_TRY(set_device(ctx));
+    SmallFp64 small(ctx);
     TB_TRY(ensure_work(ctx));
     cudaEvent_t e0;
     begin_call(ctx, &e0);
@@ -1675,37 +1763,10 @@ int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, do
     else
         TB_CUDA(cudaMemcpyAsync(s.qin, s.q0, na * 8, cudaMemcpyDeviceToDevice, st));
     TB_CUDA(cudaMemsetAsync(s.hist_meta, 0, 2 * sizeof(int32_t), st));
-    TB_CUDA(cudaMemsetAsync(w.state, 0, sizeof(DevState), st));
-    launch_coulomb_shift(st, s, s.qin, s.V, w.shift);
-    ctx->launches++;
     DevState hs;
-    std::memset(&hs, 0, sizeof(hs));
-    int it = 0, rc = TB_ERR_NOT_CONVERGED;
-    for (it = 1; it <= ctx->p.scc_max_iter; it++) {
-        bool graphed = false;
-        TB_TRY(scc_iteration(ctx, &graphed));
-        TB_CUDA(cudaGetLastError());
-        TB_TRY(read_state(ctx, hs));
-        if (graphed) {  // the replay's moment phase, timed by the graph's own events
-            float ms = 0.f;
-            if (cudaEventElapsedTime(&ms, ctx->graph_ev[0], ctx->graph_ev[1]) == cudaSuccess)
-                ctx->extra_moment_ms += ms;
-            else
-                cudaGetLastError();  // a timing gap is not an error of the solve
-        }
-        if (hs.status) {
-            rc = state_status(ctx, hs);
-            break;
-        }
-        if (hs.converged) {
-            rc = TB_OK;
-            break;
-        }
-    }
-    if (it > ctx->p.scc_max_iter) {
-        it = ctx->p.scc_max_iter;
-        fail(ctx, TB_ERR_NOT_CONVERGED, "SCC reached scc_max_iter");
-    }
+    int it = 0;
+    const int rc = scc_loop(ctx, &it, hs);
+    if (rc != TB_OK && rc != TB_ERR_NOT_CONVERGED && !(rc >= TB_ERR_SPECTRUM && rc <= TB_ERR_DIVERGED)) return rc;
     if (q) TB_CUDA(cudaMemcpyAsync(q, w.q, na * 8, cudaMemcpyDeviceToHost, st));
     if (diagP) TB_CUDA(cudaMemcpyAsync(diagP, w.diagP, n * 8, cudaMemcpyDeviceToHost, st));
     TB_CUDA(cudaStreamSynchronize(st));
@@ -1713,6 +1774,10 @@ int tb_scc_solve(tb_ctx *ctx, const double *q_init, double *q, double *diagP, do
     if (mu) *mu = hs.mu;
     if (iters) *iters = it;
     fill_report(ctx, e0, hs, it, rep);
+    if (rep && small.on) {
+        rep->fp64_evals = it;
+        rep->precision = TB_PREC_FP64;
+    }
     return rc;
     TB_ABI_CATCH
 }

@@ -297,6 +297,10 @@ int host_csr_to_bsr(int32_t n, const int32_t *rowptr, const int32_t *colidx, con
                     const int32_t *orb2atom, int32_t natoms, HostBsr &hb, std::string &err);
 int host_check_gamma(int32_t natoms, const int32_t *g_rowptr, const int32_t *g_colidx,
                      const double *g_vals, const double *q0, std::string &err);
+// tb_api.cpp: the Hamiltonian of a context from a validated host BSR (a
+// batch member solved on its own in FP64, tb_params.fp64_small)
+int set_hamiltonian_bsr(tb_ctx *ctx, int32_t n, int32_t natoms, const HostBsr &hb);
+constexpr int kSmallFp64N = 512;  // default orbital limit of tb_params.fp64_small
 
 // ---- tb_geom.cu ----------------------------------------------------------
 struct GeomDevice {

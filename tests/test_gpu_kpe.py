@@ -19,6 +19,9 @@ def _pair(nx, ny, nz, sigma=0.05, seed=1001, gamma_diag=1.0):
 
 
 def _ctx(T, m, **kw):
+    # these tests exercise the FP32 kernels on small matrices too: no FP64
+    # substitution for small structures (tb_params.fp64_small) unless asked
+    kw.setdefault("fp64_small", -1)
     c = T.Context(**kw)
     c.set_model(m)
     return c
