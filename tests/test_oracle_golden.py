@@ -172,3 +172,23 @@ def test_moments_pinned_by_reference_dos(golden):
     assert abs(tr[0] - n) < 1e-9
     z = moment_z(mu, nvec, tr, n, K)[1:]
     assert np.abs(z).max() < 5 and np.mean(z ** 2) < 2
+
+
+def test_headline_oracle_fixture_is_this_model():
+    """The committed FP64-oracle SCC of the 6x6x6 cell (tests/golden/
+    make_scc_oracle.py) was computed on the Hamiltonian the oracle builds
+    today: same size, pattern and value sums; its run converged (24
+    iterations to 1e-6 e, residual history falling to 1e-8 e) and holds the
+    electron count."""
+    import os
+    fx = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "scc_oracle_6x6x6.npz"))
+    m = O.cristobalite(6, 6, 6, sigma_ang=float(fx["sigma_ang"]), seed=int(fx["seed"]))
+    ms = fx["model_sums"]
+    assert m.n == int(ms[0]) and m.rowptr[-1] == int(ms[1])
+    np.testing.assert_allclose([np.sum(m.val), np.sum(m.val * m.val), np.sum(np.abs(m.val)), np.sum(m.xyz)],
+                               ms[2:], rtol=1e-12)
+    it = int(fx["iters"])
+    assert fx["dq_hist"][it - 1] < 1e-6 <= fx["dq_hist"][it - 2]
+    assert fx["dq_hist"][-1] < float(fx["tight_tol"])
+    assert abs(fx["q"].sum() - m.n_elec) < 1e-6
+    assert np.abs(fx["q"] - fx["q_tight"]).max() < 1e-6
