@@ -164,7 +164,6 @@ int check_kernel_flags(tb_ctx *ctx)
     }
     if (serr) {
         cudaMemsetAsync(ctx->pl.err, 0, sizeof(int32_t), ctx->stream);
-        if (serr == 3) return fail(ctx, TB_ERR_CUDA, "pipelined Chebyshev kernel: a stage held a foreign record");
         return fail(ctx, TB_ERR_TIMEOUT, serr == 2 ? "pipelined Chebyshev kernel: a neighbour-flag wait ran out"
                                                    : "pipelined Chebyshev kernel: a stage mbarrier wait ran out");
     }

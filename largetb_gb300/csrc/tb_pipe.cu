@@ -31,7 +31,7 @@
 //    tiles in step order and all CTAs are co-resident, so the oldest
 //    unfinished step can always proceed.  The pipeline never drains between
 //    steps;
-//  - the batched form (k_cheb_f32_pipe<true>, one launch per step): tiles
+//  - the batched form (k_cheb_f32_pipe<true, ...>, one launch per step): tiles
 //    come from a list over many structures, each tile naming its row group
 //    and carrying the offset of its chunk in that structure's slabs and of
 //    its column sums; a group's header holds its first (structure-local)
@@ -169,50 +169,64 @@ __device__ __forceinline__ void fence_proxy_async_global()
     asm volatile("fence.proxy.async.global;\n" ::: "memory");
 }
 
-// Warp-collective (every lane of the warp calls it, all get the same
-// answer): poll until the phase of the given parity completes; false on abort
-// or after kPipeSpin polls (then the abort and device error flags are
-// raised).  The abort test is a warp vote, so a warp never splits over it.
+// Poll until the phase of the given parity completes; false on abort or
+// after kPipeSpin polls (then the abort and device error flags are raised).
+// Each lane polls on its own; lanes may leave on an abort at different polls,
+// so a caller uses it only where a lane's answer governs that lane's own work.
 __device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t parity, volatile int *s_abort,
                                            int32_t *err)
 {
     uint32_t n = 0;
-    while (!__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) {
-        if (__any_sync(0xffffffffu, *s_abort != 0)) return false;
+    while (!mbar_try_wait(bar, parity)) {
+        if (*s_abort) return false;
         if (++n >= kPipeSpin) {
-            if ((threadIdx.x & 31) == 0) {
-                *s_abort = 1;
-                atomicExch(err, 1);
-            }
-            __syncwarp();
+            *s_abort = 1;
+            atomicExch(err, 1);
             return false;
         }
     }
     return true;
 }
 
-// Warp-collective wait of the consumers for tile i's stage.  A tile the
-// producer issued is always waited for (its bulk copies must land before the
-// stage is refilled or the CTA exits), abort or not; a tile the producer never
-// issued (*s_issued: -1 while it runs, then the count it issued) is given up.
-// That test comes before the barrier poll: once the consumers pass over a
-// phase that never completed, a later poll of the same stage can name a
-// parity that an older, completed phase had, and try_wait would report the
-// never-filled stage as full.  Bounded by kPipeSpin polls like every wait.
-__device__ __forceinline__ bool wait_full(uint64_t *bar, uint32_t parity, int i, volatile int *s_abort,
-                                          volatile int *s_issued, int32_t *err)
+// wait_phase with the warp's answer: every lane of the warp calls it and all
+// get the same result, so a warp never splits over an abort.  For the
+// producer (its copy issue is one warp-wide step), the publisher and the
+// publisher hand-off.
+__device__ __forceinline__ bool wait_phase_warp(uint64_t *bar, uint32_t parity, volatile int *s_abort,
+                                                int32_t *err)
 {
+    return __all_sync(0xffffffffu, wait_phase(bar, parity, s_abort, err));
+}
+
+// The consumers' wait for tile i's stage (per lane, like wait_phase).  A tile
+// the producer issued is always waited for (its bulk copies must land before
+// the stage is refilled or the CTA exits), abort or not; a tile the producer
+// never issued (*s_issued: -1 while it runs, then the count it issued) is
+// given up, and so is every later one (gave_up): once a lane has passed over
+// a phase that never completed, a later poll of that stage could name a
+// parity that an older, completed phase had, and try_wait would report a
+// never-filled stage as full.  Until then no phase was skipped, so a poll
+// that succeeds is the tile's own phase.  Every lane reaches the same verdict
+// (a never-issued tile never completes, an issued one always does).  The
+// issue count is looked at once every 64 unsuccessful polls, keeping the
+// common path to the poll alone.  Bounded by kPipeSpin polls like every wait.
+__device__ __forceinline__ bool wait_full(uint64_t *bar, uint32_t parity, int i, volatile int *s_abort,
+                                          volatile int *s_issued, int32_t *err, bool &gave_up)
+{
+    if (gave_up) return false;
     uint32_t n = 0;
-    for (;;) {
-        const int iss = __shfl_sync(0xffffffffu, *s_issued, 0);
-        if (iss >= 0 && i >= iss) return false;
-        if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
-        if (++n >= kPipeSpin) {
-            if ((threadIdx.x & 31) == 0) {
-                *s_abort = 1;
-                atomicExch(err, 1);
+    while (!mbar_try_wait(bar, parity)) {
+        if ((++n & 63u) == 0u) {
+            const int iss = *s_issued;
+            if (iss >= 0 && i >= iss) {
+                gave_up = true;
+                return false;
             }
-            __syncwarp();
+        }
+        if (n >= kPipeSpin) {
+            *s_abort = 1;
+            atomicExch(err, 1);
+            gave_up = true;
             return false;
         }
     }
@@ -261,17 +275,20 @@ __device__ __forceinline__ bool wait_neighbours(const PipeArgs &a, int chunk, in
 // Tile of this CTA's i-th task.  One-launch-per-step launches sweep the
 // tiles backwards on odd steps, so a step starts on the rows of T_{k+1} and
 // T_k that the previous step touched last and that are still in L2.
+template <bool kMulti>
 __device__ __forceinline__ int tile_of_task(const PipeArgs &a, int ntiles, int i, int mine)
 {
     const int t = (int)blockIdx.x + (i % mine) * (int)gridDim.x;
     const int k = a.k0 + i / mine;
-    return (!a.flags && (k & 1)) ? ntiles - 1 - t : t;
+    return (!kMulti && (k & 1)) ? ntiles - 1 - t : t;
 }
 
 // kBatch: tiles come from a.tiles (row groups of many structures, each
 // structure its own chunk-major slabs and partial block); else tile t is
-// (chunk t / G, group t % G) of one slab.
-template <bool kBatch>
+// (chunk t / G, group t % G) of one slab.  kMulti: the one-launch-per-slab
+// mode (step flags, neighbour waits, the publisher warp); the per-step and
+// batched instantiations carry none of that code.
+template <bool kBatch, bool kMulti>
 __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -314,13 +331,13 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         // the consumers' T_{k+1} stores (ordered before the slot's mbarrier
         // arrival) visible before the release store of the flag.  The fence
         // stalls only this warp.
-        if (!a.flags) return;
+        if constexpr (!kMulti) return;
         for (int i = 0; i < total; ++i) {
             const int s = i % kPubSlots;
-            if (!wait_phase(&pub[s], (uint32_t)(i / kPubSlots) & 1u, s_abort, a.err)) break;
+            if (!wait_phase_warp(&pub[s], (uint32_t)(i / kPubSlots) & 1u, s_abort, a.err)) break;
             if (lane == 0) {
                 const int k = a.k0 + i / mine;
-                const int t = tile_of_task(a, ntiles, i, mine);
+                const int t = tile_of_task<kMulti>(a, ntiles, i, mine);
                 __threadfence();
                 fence_proxy_async_global();
                 if (t != a.stall_tile) st_release(a.flags + t, k + 1);
@@ -339,11 +356,11 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         int64_t cnext = 0;      // batched form: its chunk offset
         if (total > 0) {
             if constexpr (kBatch) {
-                const int t0 = tile_of_task(a, ntiles, 0, mine);
+                const int t0 = tile_of_task<kMulti>(a, ntiles, 0, mine);
                 gnext = a.tiles[t0].g;
                 cnext = a.tiles[t0].coff;
             } else {
-                gnext = tile_of_task(a, ntiles, 0, mine) % a.G;
+                gnext = tile_of_task<kMulti>(a, ntiles, 0, mine) % a.G;
             }
             ha = __ldg(a.hdr + 2 * gnext);
             hb = __ldg(a.hdr + 2 * gnext + 1);
@@ -351,7 +368,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         }
         for (; i < total; ++i) {
             const int k = a.k0 + i / mine;
-            const int t = tile_of_task(a, ntiles, i, mine);
+            const int t = tile_of_task<kMulti>(a, ntiles, i, mine);
             const int g = gnext;
             const int chunk = kBatch ? 0 : t / a.G;
             const int64_t coff = kBatch ? cnext : (int64_t)chunk * chunk_floats;
@@ -359,7 +376,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
             const int rl = hb.x, I0 = hb.y, nruns = hb.z, nr = hb.w;
             const int4 cur = run;
             if (i + 1 < total) {  // header and runs of the next tile
-                const int tn = tile_of_task(a, ntiles, i + 1, mine);
+                const int tn = tile_of_task<kMulti>(a, ntiles, i + 1, mine);
                 if constexpr (kBatch) {
                     gnext = a.tiles[tn].g;
                     cnext = a.tiles[tn].coff;
@@ -372,19 +389,17 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
             }
             // this tile's neighbour flags, read before the stage wait
             int seen = 0x7fffffff;
-            if (a.flags && k > 0) {
+            if (kMulti && k > 0) {
                 const int32_t *f = neighbour_flag(a, chunk, g, lane);
                 if (f) seen = ld_acquire(f);
             }
             const int s = i % a.stages;
-            if (i >= a.stages && !wait_phase(&empty[s], (uint32_t)((i / a.stages) - 1) & 1u, s_abort, a.err))
+            if (i >= a.stages && !wait_phase_warp(&empty[s], (uint32_t)((i / a.stages) - 1) & 1u, s_abort, a.err))
                 break;
-            if (a.flags && k > 0) {
+            if (kMulti && k > 0) {
                 if (!wait_neighbours(a, chunk, g, k, lane, seen, s_abort)) break;
                 fence_proxy_async_global();
             }
-            // no copy is issued once any warp of the CTA has given up
-            if (__any_sync(0xffffffffu, *s_abort != 0)) break;
             const float *Tin = (k & 1) ? a.T1 : a.T0;
             const float *Tprev = (k & 1) ? a.T0 : a.T1;
             float *stg = reinterpret_cast<float *>(smem + (size_t)s * a.stage_bytes);
@@ -427,9 +442,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
 
     // ---------------- consumers ----------------
     const int c = 2 * lane;
+    bool gave_up = false;  // this warp has passed over a tile that was never issued
     for (int i = 0; i < total; ++i) {
         const int k = a.k0 + i / mine;
-        const int t = tile_of_task(a, ntiles, i, mine);
+        const int t = tile_of_task<kMulti>(a, ntiles, i, mine);
         const int s = i % a.stages;
         int g, I0, nr;
         int64_t coff, pbase;  // slab offset of the tile's chunk; float2 offset of its column sums
@@ -453,16 +469,13 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         // pairs (hi, lo), packed over columns (c, c+1): <T_k,T_k> in (eh, el),
         // <T_k,T_{k+1}> in (oh, ol)
         float2 eh = make_float2(0.f, 0.f), el = eh, oh = eh, ol = eh;
-        if (wait_full(&full[s], (uint32_t)(i / a.stages) & 1u, i, s_abort, s_issued, a.err)) {
+        if (wait_full(&full[s], (uint32_t)(i / a.stages) & 1u, i, s_abort, s_issued, a.err, gave_up)) {
             const float *stg = reinterpret_cast<const float *>(smem + (size_t)s * a.stage_bytes);
             const float *sT = stg + oT, *sP = stg + oP, *sX = stg + oX;
             const int32_t *sRp = reinterpret_cast<const int32_t *>(stg + oRec);
             const int32_t *sLc = sRp + nr + 1;
             const int32_t *sLs = sLc + sRp[nr];
-            // a stage whose record does not describe this tile is never used
-            const bool rec_ok = sRp[0] == 0 && sRp[nr] >= 0 && sRp[nr] <= a.maxBlk;
-            if (!rec_ok && lane == 0) atomicExch(a.err, 3);
-            for (int r = rec_ok ? warp : nr; r < nr; r += kPipeCW) {
+            for (int r = warp; r < nr; r += kPipeCW) {
                 // acc[q] = row q of the block row, columns (c, c+1)
                 float2 acc[4];
 #pragma unroll
@@ -524,10 +537,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
             if (lane == 0) mbar_arrive(redfree);
             // the first reducer hands the tile to the publisher: it has seen every
             // consumer warp's arrival, so all stores of the tile precede this
-            if (a.flags && rw == 0) {
+            if (kMulti && rw == 0) {
                 const int ps = i % kPubSlots;
                 if (i < kPubSlots ||
-                    wait_phase(&pubfree[ps], (uint32_t)((i / kPubSlots) - 1) & 1u, s_abort, a.err)) {
+                    wait_phase_warp(&pubfree[ps], (uint32_t)((i / kPubSlots) - 1) & 1u, s_abort, a.err)) {
                     if (lane == 0) mbar_arrive(&pub[ps]);
                 }
             }
@@ -591,11 +604,16 @@ int cheb_f32_pipe_max_rows() { return kPipeCW * 3; }
 
 int cheb_f32_pipe_configure(size_t smem, int *ctas_per_sm, bool batch)
 {
-    const void *fn = batch ? (const void *)k_cheb_f32_pipe<true> : (const void *)k_cheb_f32_pipe<false>;
+    const void *fn = batch ? (const void *)k_cheb_f32_pipe<true, false> : (const void *)k_cheb_f32_pipe<false, false>;
     const int lim = smem_optin_max(fn);
     if ((int)smem > lim) return (int)cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (e != cudaSuccess) return (int)e;
+    if (!batch) {
+        const void *fm = (const void *)k_cheb_f32_pipe<false, true>;
+        if ((e = cudaFuncSetAttribute(fm, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin_max(fm))))
+            return (int)e;
+    }
     *ctas_per_sm = 0;
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, kPipeThreads, smem);
 }
@@ -657,13 +675,13 @@ int launch_cheb_f32_pipe(cudaStream_t st, const DevMatrix &m, const PipePlan &pl
     const int grid = std::min(ntiles, pl.nsm);
     const size_t smem = cheb_f32_pipe_smem(pl.stage_bytes, pl.stages);
     if (!multi) {
-        k_cheb_f32_pipe<false><<<grid, kPipeThreads, smem, st>>>(a);
+        k_cheb_f32_pipe<false, false><<<grid, kPipeThreads, smem, st>>>(a);
         return (int)cudaSuccess;
     }
     cudaError_t e = cudaMemsetAsync(pl.flags, 0, sizeof(int32_t) * (size_t)ntiles, st);
     if (e != cudaSuccess) return (int)e;
     void *args[] = {&a};
-    return (int)cudaLaunchCooperativeKernel((const void *)k_cheb_f32_pipe<false>, dim3(grid), dim3(kPipeThreads), args,
+    return (int)cudaLaunchCooperativeKernel((const void *)k_cheb_f32_pipe<false, true>, dim3(grid), dim3(kPipeThreads), args,
                                             smem, st);
 }
 
@@ -695,7 +713,7 @@ void launch_cheb_f32_pipe_batch(cudaStream_t st, const PipePlan &pl, const PipeB
     a.stall_tile = -1;
     const int grid = std::min(ntiles, pl.nsm);
     if (grid < 1) return;
-    k_cheb_f32_pipe<true><<<grid, kPipeThreads, cheb_f32_pipe_smem(pl.stage_bytes, pl.stages), st>>>(a);
+    k_cheb_f32_pipe<true, false><<<grid, kPipeThreads, cheb_f32_pipe_smem(pl.stage_bytes, pl.stages), st>>>(a);
 }
 
 }  // namespace tb
