@@ -414,6 +414,10 @@ def run_all_kernels(T, dev):
         c.set_model(T.model_cristobalite(2, 2, 2, sigma_ang=0.08, seed=3))
         c.sp2()
     calls.append("sp2 x6")
+    with T.Context(M=60, kT=0.0, precision=T.PREC_FP64, device=dev) as c:
+        c.set_model(T.model_cristobalite(2, 2, 2, sigma_ang=0.05, seed=5))
+        c.density_stochastic(n_probes=16, seed=3, dos_moments=100, dos_points=200)
+    calls.append("stochastic density (16 probes)")
     with T.Context(M=60, device=dev) as c:
         c.set_geometry(m.xyz, m.species, learned.cell_box((3, 3, 3)), rcut_bohr=4.0, gamma_diag=1.0)
         c.density()
