@@ -1103,12 +1103,12 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
     // tb_params.fp64_small: small members leave the batch and are solved on
     // their own with the plain FP64 recurrence (launch-bound either way)
     const int small_n = b->p.fp64_small == 0 ? kSmallFp64N : b->p.fp64_small;
-    std::vector<char> pol_done(S, 0);
-    std::vector<int> pol_rc(S, TB_OK), pol_it(S, 0);
-    std::vector<DevState> pol_hs(S);
-    std::vector<std::vector<double>> pol_q(S);
-    std::vector<std::string> pol_err(S);
-    int64_t polish_evals = 0;
+    std::vector<char> small_done(S, 0);
+    std::vector<int> small_rc(S, TB_OK);
+    std::vector<DevState> small_hs(S);
+    std::vector<std::vector<double>> small_q(S);
+    std::vector<std::string> small_err(S);
+    int64_t small_evals = 0;
     for (int s = 0; s < S && small_n > 0; s++) {
         const int na_s = b->h_ao[s + 1] - b->h_ao[s];
         if (4 * na_s > small_n) continue;
@@ -1118,22 +1118,21 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
         pp.n_electrons = 0.0;   // sum(q0) of this structure
         tb_ctx *c = nullptr;
         int prc = tb_ctx_create(&pp, &c);
-        if (prc != TB_OK) pol_err[s] = std::string("context: ") + tb_status_string(prc);
+        if (prc != TB_OK) small_err[s] = std::string("context: ") + tb_status_string(prc);
         if (prc == TB_OK) prc = set_hamiltonian_bsr(c, 4 * na_s, na_s, b->hb[s]);
         if (prc == TB_OK)
             prc = tb_set_scc(c, na_s, b->grp[s].data(), b->gci[s].data(), b->gv[s].data(), b->q0[s].data());
-        pol_q[s].assign(na_s, 0.0);
+        small_q[s].assign(na_s, 0.0);
         int32_t its = 0;
         if (prc == TB_OK)
-            prc = tb_scc_solve(c, q_init ? q_init + b->h_ao[s] : nullptr, pol_q[s].data(), nullptr,
-                               &pol_hs[s].e_band, &pol_hs[s].mu, &its, nullptr);
-        if (prc != TB_OK && c) pol_err[s] = tb_last_error(c);
+            prc = tb_scc_solve(c, q_init ? q_init + b->h_ao[s] : nullptr, small_q[s].data(), nullptr,
+                               &small_hs[s].e_band, &small_hs[s].mu, &its, nullptr);
+        if (prc != TB_OK && c) small_err[s] = tb_last_error(c);
         if (c) tb_ctx_destroy(c);
-        pol_hs[s].converged = prc == TB_OK;
-        pol_rc[s] = prc == TB_ERR_NOT_CONVERGED ? TB_OK : prc;  // the cap is reported below
-        pol_it[s] = its;
-        pol_done[s] = 1;
-        polish_evals += its;
+        small_hs[s].converged = prc == TB_OK;
+        small_rc[s] = prc == TB_ERR_NOT_CONVERGED ? TB_OK : prc;  // the cap is reported below
+        small_done[s] = 1;
+        small_evals += its;
         conv_iter[s] = its;
         act[s] = 0;
     }
@@ -1313,8 +1312,8 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
     cudaEventSynchronize(e1);
     if (q)
         for (int s = 0; s < S; s++)
-            if (pol_done[s] && pol_rc[s] == TB_OK)
-                std::copy(pol_q[s].begin(), pol_q[s].end(), q + b->h_ao[s]);
+            if (small_done[s] && small_rc[s] == TB_OK)
+                std::copy(small_q[s].begin(), small_q[s].end(), q + b->h_ao[s]);
     float tot = 0.f;
     cudaEventElapsedTime(&tot, e0, e1);
     cudaEventDestroy(e0);
@@ -1330,12 +1329,12 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
         }
     }
     for (int s = 0; s < S; s++)
-        if (pol_done[s]) hs[s] = pol_hs[s];
+        if (small_done[s]) hs[s] = small_hs[s];
     if (rc == TB_OK) {
         for (int s = 0; s < S; s++) {
-            if (pol_done[s] && pol_rc[s] != TB_OK) {
-                rc = pol_rc[s];
-                b->err = "structure " + std::to_string(s) + " (FP64 polish): " + pol_err[s];
+            if (small_done[s] && small_rc[s] != TB_OK) {
+                rc = small_rc[s];
+                b->err = "structure " + std::to_string(s) + " (solved alone in FP64): " + small_err[s];
                 break;
             }
             if (hs[s].status) {
@@ -1364,7 +1363,7 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
         rep->kernel_launches = launches;
         rep->precision = TB_PREC_FP32;
         rep->column_block = -1;
-        rep->fp64_evals = (int32_t)polish_evals;
+        rep->fp64_evals = (int32_t)small_evals;
     }
     return rc;
     TB_ABI_CATCH
