@@ -406,7 +406,7 @@ int ensure_work(tb_ctx *ctx)
     TB_TRY(dalloc(ctx, w.d, (size_t)(M + 1) * m.n));
     TB_TRY(dalloc(ctx, w.mom, (size_t)M + 1));
     TB_TRY(dalloc(ctx, w.c, (size_t)M));
-    TB_TRY(dalloc(ctx, w.rho, (size_t)w.nq_cap));
+    TB_TRY(dalloc(ctx, w.rho, 2 * (size_t)w.nq_cap));  // DOS at the nodes, then e^{beta x_q}
     TB_TRY(dalloc(ctx, w.fq, (size_t)w.nq_cap));
     TB_TRY(dalloc(ctx, w.costab, 4 * (size_t)w.nq_cap));
     launch_cos_table(ctx->stream, w.nq_cap, w.costab);

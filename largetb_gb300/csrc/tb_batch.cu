@@ -41,6 +41,9 @@ constexpr double kPi = 3.141592653589793238463;
 constexpr int kBtCols = 64;
 constexpr int kBtWarps = 8;
 constexpr int kBtR = 24;  // block rows per group (one beta-cristobalite cell)
+// Below this beta_x the multisection uses e^{beta x_q} e^{-beta mu} (|t| <= 600,
+// inside the FP64 range) instead of one exp per node and candidate.
+constexpr double kBtEtabBeta = 300.0;
 
 __device__ __forceinline__ double wsum(double v)
 {
@@ -321,7 +324,8 @@ __global__ void __launch_bounds__(256)
 // mod 4 nq) r], r = nq > 0 ? nq_cap / nq : 1, as in the single-structure kernels.
 __global__ void k_bt_dos_nodes(const double *__restrict__ g, const double *__restrict__ mom, int M,
                                const DevState *__restrict__ st, const int32_t *__restrict__ active,
-                               int nq_cap, const double *__restrict__ tab, double *__restrict__ rho)
+                               int nq_cap, const double *__restrict__ tab, double *__restrict__ rho,
+                               double *__restrict__ ebx)
 {
     extern __shared__ double wk[];  // (2 - delta_k0) g_k mu_k of this structure
     const int s = blockIdx.y;
@@ -341,6 +345,9 @@ __global__ void k_bt_dos_nodes(const double *__restrict__ g, const double *__res
             v += wk[kk] * tab[((size_t)j * r) & cmask];
         }
         rho[(int64_t)s * nq_cap + q] = v;
+        // e^{beta_x x_q} for the multisection; unused above kBtEtabBeta
+        const double bx = st[s].beta_x;
+        ebx[(int64_t)s * nq_cap + q] = bx <= kBtEtabBeta ? exp(bx * tab[((size_t)step * r) & cmask]) : 0.0;
     }
 }
 
@@ -359,7 +366,8 @@ __global__ void k_bt_fermi_nodes(const DevState *__restrict__ st_all, const int3
 }
 
 __global__ void __launch_bounds__(256)
-    k_bt_bisect(const double *__restrict__ rho, int nq_cap, const double *__restrict__ tab,
+    k_bt_bisect(const double *__restrict__ rho, const double *__restrict__ ebx, int nq_cap,
+                const double *__restrict__ tab,
                 const double *__restrict__ g,
                 const double *__restrict__ mom, int M, const double *__restrict__ n_elec, double tol_n,
                 int round, int last_round, const int32_t *__restrict__ active, double *__restrict__ cand,
@@ -378,8 +386,14 @@ __global__ void __launch_bounds__(256)
         const int nq = st->nq, r = nq > 0 ? nq_cap / nq : 1;
         const size_t cmask = 4 * (size_t)nq_cap - 1;  // keeps every table index in range
         const double *rs = rho + (int64_t)s * nq_cap;
-        for (int q = threadIdx.x; q < nq; q += blockDim.x)
-            v += fermi_d(tab[((size_t)(2 * q + 1) * r) & cmask], mu, beta) * rs[q];
+        if (beta <= kBtEtabBeta) {
+            // f(x_q) = 1 / (1 + e^{beta x_q} e^{-beta mu}): one exp per candidate
+            const double C = exp(-beta * mu), *eb = ebx + (int64_t)s * nq_cap;
+            for (int q = threadIdx.x; q < nq; q += blockDim.x) v += rs[q] / (1.0 + eb[q] * C);
+        } else {
+            for (int q = threadIdx.x; q < nq; q += blockDim.x)
+                v += fermi_d(tab[((size_t)(2 * q + 1) * r) & cmask], mu, beta) * rs[q];
+        }
         v = 2.0 * bsum(v, sh) / nq;
     } else {
         const double th = acos(mu);
@@ -699,6 +713,7 @@ struct tb_batch {
     double *h0 = nullptr, *h0diag = nullptr, *radius = nullptr, *d = nullptr, *mom = nullptr, *c = nullptr;
     double *g = nullptr, *rho = nullptr, *cand = nullptr, *diagP = nullptr, *q = nullptr, *partial = nullptr;
     double *fq = nullptr, *costab = nullptr;  // Fermi function at the nodes [S][nq_cap]; cosine table 4 nq_cap
+    double *ebx = nullptr;                      // e^{beta_x x_q} at the nodes [S][nq_cap]
     double *g_v = nullptr, *q0d = nullptr, *qin = nullptr, *shift = nullptr, *hq = nullptr, *hr = nullptr;
     double *ne = nullptr;
     float *x32 = nullptr, *xdiag32 = nullptr, *T0 = nullptr, *T1 = nullptr;
@@ -942,6 +957,7 @@ int batch_build(tb_batch *b)
     BT(balloc(b, b->c, (size_t)S * M));
     BT(balloc(b, b->rho, (size_t)S * nq_cap));
     BT(balloc(b, b->fq, (size_t)S * nq_cap));
+    BT(balloc(b, b->ebx, (size_t)S * nq_cap));
     BT(balloc(b, b->costab, 4 * (size_t)nq_cap));
     launch_cos_table(b->stream, nq_cap, b->costab);
     BT(balloc(b, b->cand, (size_t)S * kBisectCand));
@@ -1236,9 +1252,9 @@ int tb_batch_scc_solve(tb_batch *b, const double *q_init, double *q, int32_t *it
             k_bt_moment_sums<<<dim3(M + 1, S), 256, 0, st>>>(b->d, n, M, b->s_ao, b->active, b->mom);
             if (b->p.kT > 0)
                 k_bt_dos_nodes<<<dim3(64, S), 256, sizeof(double) * M, st>>>(b->g, b->mom, M, b->st, b->active,
-                                                                             b->nq_cap, b->costab, b->rho);
+                                                                             b->nq_cap, b->costab, b->rho, b->ebx);
             for (int r = 0; r < kBisectRounds; r++)
-                k_bt_bisect<<<dim3(kBisectCand, S), 256, 0, st>>>(b->rho, b->nq_cap, b->costab, b->g, b->mom, M,
+                k_bt_bisect<<<dim3(kBisectCand, S), 256, 0, st>>>(b->rho, b->ebx, b->nq_cap, b->costab, b->g, b->mom, M,
                                                                   b->ne, b->p.mu_tol, r, kBisectRounds - 1,
                                                                   b->active, b->cand, b->st);
             k_bt_fermi_nodes<<<dim3(16, S), 256, 0, st>>>(b->st, b->active, b->nq_cap, b->costab, b->fq);

@@ -135,7 +135,7 @@ struct DevWork {
     double *mom = nullptr;     // M+1
     double *g = nullptr;       // M damping factors
     double *c = nullptr;       // M expansion coefficients
-    double *rho = nullptr;     // nq damped DOS at the quadrature nodes
+    double *rho = nullptr;     // [2 nq_cap]: damped DOS at the nodes, then e^{beta_x x_q}
     double *fq = nullptr;      // nq Fermi function at the quadrature nodes
     double *costab = nullptr;  // 4 nq_cap: cos(pi j / (2 nq_cap)), see k_cos_table
     double *cand = nullptr;    // kBisectCand electron counts

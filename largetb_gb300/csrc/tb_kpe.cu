@@ -70,6 +70,10 @@ __device__ double block_sum(double v, double *sh)
     return r;
 }
 
+// Above this beta_x the multisection evaluates the Fermi function node by node;
+// below it e^{beta x} e^{-beta mu} stays far inside the FP64 range (|t| <= 600).
+constexpr double kEtabBeta = 300.0;
+
 __device__ __forceinline__ double fermi(double x, double mu_x, double beta_x)
 {
     const double t = beta_x * (x - mu_x);
@@ -885,7 +889,7 @@ void launch_cos_table(cudaStream_t st, int nq_cap, double *tab)
 // the Chebyshev-Gauss nodes (times pi sin theta), nq read from the state.
 __global__ void k_dos_nodes(const double *__restrict__ g, const double *__restrict__ mom, int M,
                             const DevState *__restrict__ st, int nq_cap, const double *__restrict__ tab,
-                            double *__restrict__ rho)
+                            double *__restrict__ rho, double *__restrict__ ebx)
 {
     extern __shared__ double wk[];  // (2 - delta_k0) g_k mu_k
     for (int k = threadIdx.x; k < M; k += blockDim.x) wk[k] = k == 0 ? g[0] * mom[0] : 2.0 * g[k] * mom[k];
@@ -902,6 +906,9 @@ __global__ void k_dos_nodes(const double *__restrict__ g, const double *__restri
             s += wk[k] * tab[((size_t)j * r) & cmask];
         }
         rho[q] = s;
+        // e^{beta_x x_q} for the multisection; unused above kEtabBeta
+        const double bx = st->beta_x;
+        ebx[q] = bx <= kEtabBeta ? exp(bx * tab[((size_t)step * r) & cmask]) : 0.0;
     }
 }
 
@@ -911,7 +918,7 @@ void launch_dos_nodes(cudaStream_t st, const double *g, const double *mom, int M
     const int T = 256;
     int blocks = (nq_cap + T - 1) / T;
     if (blocks > 1024) blocks = 1024;
-    k_dos_nodes<<<blocks, T, sizeof(double) * M, st>>>(g, mom, M, state, nq_cap, tab, rho);
+    k_dos_nodes<<<blocks, T, sizeof(double) * M, st>>>(g, mom, M, state, nq_cap, tab, rho, rho + nq_cap);
 }
 
 // ---------------------------------------------------------------------------
@@ -937,8 +944,15 @@ __global__ void __launch_bounds__(256)
         const int nq = st->nq;
         const int r = nq > 0 ? nq_cap / nq : 1;
         const size_t cmask = 4 * (size_t)nq_cap - 1;  // keeps every table index in range
-        for (int q = threadIdx.x; q < nq; q += blockDim.x)
-            s += fermi(tab[((size_t)(2 * q + 1) * r) & cmask], mu, beta_x) * rho[q];
+        if (beta_x <= kEtabBeta) {
+            // f(x_q) = 1 / (1 + e^{beta x_q} e^{-beta mu}): one exp per candidate,
+            // the node factors from k_dos_nodes (no overflow below kEtabBeta)
+            const double C = exp(-beta_x * mu), *ebx = rho + nq_cap;
+            for (int q = threadIdx.x; q < nq; q += blockDim.x) s += rho[q] / (1.0 + ebx[q] * C);
+        } else {
+            for (int q = threadIdx.x; q < nq; q += blockDim.x)
+                s += fermi(tab[((size_t)(2 * q + 1) * r) & cmask], mu, beta_x) * rho[q];
+        }
         s = block_sum(s, sh);
         s = 2.0 * s / nq;
     } else {
