@@ -292,14 +292,29 @@ __global__ void k_bt_finalize(int n_total, int k, int M, const int32_t *__restri
     const int s = s_of_atom[i >> 2];
     if (!active[s]) return;
     const int j = i - 4 * s_ao[s], B = s_B[s], G = s_g0[s + 1] - s_g0[s];
-    const float2 *p = partial + s_poff[s];
+    // (e, o) of column j in group g: one 16-byte load at [g][B][2] float2
+    // (s_poff is even, so the base stays 16-byte aligned)
+    const float4 *p = reinterpret_cast<const float4 *>(partial + s_poff[s]) + j;
     float eh = 0.f, el = 0.f, oh = 0.f, ol = 0.f;
-    for (int g = 0; g < G; g++) {
-        const float2 e = p[((int64_t)g * B + j) * 2 + 0], o = p[((int64_t)g * B + j) * 2 + 1];
-        pair_add(eh, el, e.x);
-        el += e.y;
-        pair_add(oh, ol, o.x);
-        ol += o.y;
+    int g = 0;
+    for (; g + 8 <= G; g += 8) {
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) v[u] = __ldg(p + (int64_t)(g + u) * B);
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            pair_add(eh, el, v[u].x);
+            el += v[u].y;
+            pair_add(oh, ol, v[u].z);
+            ol += v[u].w;
+        }
+    }
+    for (; g < G; g++) {
+        const float4 v = __ldg(p + (int64_t)g * B);
+        pair_add(eh, el, v.x);
+        el += v.y;
+        pair_add(oh, ol, v.z);
+        ol += v.w;
     }
     const double se = (double)eh + (double)el, so = (double)oh + (double)ol;
     if (2 * k <= M) d[(int64_t)(2 * k) * n_total + i] = 2.0 * se - 1.0;

@@ -560,6 +560,33 @@ __global__ void k_slab_identity_cm(float *__restrict__ T0, int n, int B, int c0)
     }
 }
 
+// Sum of (hi, lo) pairs over groups g = 0 .. G-1 at p[g * stride], in group
+// order, eight 16-byte loads in flight before their additions.
+__device__ __forceinline__ void sum_group_pairs(const float4 *__restrict__ p, int64_t stride, int G, float &eh,
+                                                float &el, float &oh, float &ol)
+{
+    int g = 0;
+    for (; g + 8 <= G; g += 8) {
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) v[u] = __ldg(p + (g + u) * stride);
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            pair_add(eh, el, v[u].x);
+            el += v[u].y;
+            pair_add(oh, ol, v[u].z);
+            ol += v[u].w;
+        }
+    }
+    for (; g < G; g++) {
+        const float4 v = __ldg(p + g * stride);
+        pair_add(eh, el, v.x);
+        el += v.y;
+        pair_add(oh, ol, v.z);
+        ol += v.w;
+    }
+}
+
 // Sum the per-group (hi, lo) pairs of a slab in FP32 pairs, convert once to
 // FP64 and form the moments d[2k][j] = 2 <T_k,T_k>_j - 1,
 // d[2k+1][j] = 2 <T_k,T_{k+1}>_j - X_jj.
@@ -572,14 +599,9 @@ __global__ void k_f32_finalize_pairs(const float2 *__restrict__ partial, int K, 
     const int i = c0 + j;
     if (i >= n) return;
     float eh = 0.f, el = 0.f, oh = 0.f, ol = 0.f;
-    const float2 *p = partial + (int64_t)k * rowgroups * B * 2;
-    for (int g = 0; g < rowgroups; g++) {
-        const float2 e = p[((int64_t)g * B + j) * 2 + 0], o = p[((int64_t)g * B + j) * 2 + 1];
-        pair_add(eh, el, e.x);
-        el += e.y;
-        pair_add(oh, ol, o.x);
-        ol += o.y;
-    }
+    // (e, o) of column j in group g: one 16-byte load at [g][B][2] float2
+    const float4 *p = reinterpret_cast<const float4 *>(partial + (int64_t)k * rowgroups * B * 2) + j;
+    sum_group_pairs(p, B, rowgroups, eh, el, oh, ol);
     const double se = (double)eh + (double)el, so = (double)oh + (double)ol;
     if (2 * k <= M) d[(int64_t)(2 * k) * n + i] = 2.0 * se - 1.0;
     if (2 * k + 1 <= M) d[(int64_t)(2 * k + 1) * n + i] = 2.0 * so - (double)xdiag32[i];
