@@ -304,6 +304,44 @@ def run_batch_bench(args, T, dev, rank):
     return out
 
 
+# The reference's own stage times on its own workload (testrun_scf2:2,6,8):
+# alpha-quartz 8x8x8 (4608 atoms, 18432 orbitals), 500 random vectors, on
+# about 64 Cray XE cores (18432 orbitals / 288 local rows, testrun_scf2:4).
+REFERENCE_LOGGED = {"log": "testrun_scf2", "kpm_dos_s": 43.2715, "first_density_s": 13.7305,
+                    "ranks_inferred": 64, "machine": "Blue Waters Cray XE (FP64 PETSc)"}
+
+
+def run_reference_stages(args, T, dev, rank):
+    """The reference's two logged stages, on the workload of its log: runKPM
+    (500 Gaussian vectors x 1000 Jackson moments of 8x8x8 alpha-quartz,
+    withSP2_deltaH.cpp:1579-1648) against tb_kpm_dos with the same sizes,
+    and computeDensityMatrix (1401-1412: computeAlphas' SP2 traces and
+    computeDiagonalElements, 500 vectors each through getKPE at M = 200 with
+    step coefficients, 1068-1399) against the density part of
+    tb_density_stochastic (mu from the DOS area, the interval refined from
+    its support, 500 probes at M = 200, kT = 0), FP64, on one GPU, times
+    from CUDA events."""
+    m = T.model_quartz(8, 8, 8)
+    c = T.Context(M=200, kT=0.0, precision=T.PREC_FP64, device=dev)
+    c.set_model(m)
+    c.kpm_dos(n_moments=1000, n_random=500, seed=1, npts=2000)  # warm-up
+    l2_flush(dev)
+    t_kpm = c.kpm_dos(n_moments=1000, n_random=500, seed=2, npts=2000)["report"]["t_total_ms"] / 1e3
+    l2_flush(dev)
+    r = c.density_stochastic(n_probes=500, seed=3, dos_moments=1000, dos_points=2000)
+    c.close()
+    t_all = r["report"]["t_total_ms"] / 1e3
+    ref = REFERENCE_LOGGED
+    return {"metric": "s per stage, the reference's logged workload (8x8x8 alpha-quartz, 500 vectors)",
+            "config": {"cells": [8, 8, 8], "atoms": m.natoms, "orbitals": m.n, "vectors": 500,
+                       "dos_moments": 1000, "M": 200, "kT": 0.0, "precision": "fp64"},
+            "kpm_dos_s": t_kpm, "density_s": t_all - t_kpm, "dos_plus_density_s": t_all,
+            "electrons": float(r["q"].sum()), "n_electrons": m.n_electrons,
+            "reference_logged": ref,
+            "ratio_kpm_dos": ref["kpm_dos_s"] / t_kpm,
+            "ratio_density": ref["first_density_s"] / max(t_all - t_kpm, 1e-9)}
+
+
 def run_learned_eval(args, T, dev, rank):
     """Learned SCC start on an 8x8x8 cell (12288 atoms, 49152 orbitals),
     sigma 0.08 A, M = 200 (the training M), FP32 form: iterations and time to
@@ -457,6 +495,8 @@ def main():
                     help="time single density evaluations (the unit profiled with ncu)")
     ap.add_argument("--zero-start", action="store_true",
                     help="start the timed solves from q0 instead of the learned charges")
+    ap.add_argument("--reference-stages", action="store_true",
+                    help="the reference's logged stages on its own workload (8x8x8 alpha-quartz)")
     ap.add_argument("--learned-eval", action="store_true",
                     help="8x8x8 cell (12288 atoms): SCC from q0 vs from the learned start (M = 200)")
     ap.add_argument("--batch", action="store_true",
@@ -487,6 +527,11 @@ def main():
         return
     if args.batch:
         run_batch_bench(args, T, dev, rank)
+        return
+    if args.reference_stages:
+        out = run_reference_stages(args, T, dev, rank)
+        if rank == 0:
+            print(json.dumps(out), flush=True)
         return
     if args.learned_eval:
         run_learned_eval(args, T, dev, rank)
@@ -669,6 +714,7 @@ def main():
         line["sp2_4x4x4"] = run_sp2_bench(sub, T, dev, rank)
         line["batch_64_cells"] = run_batch_bench(sub, T, dev, rank)
         line["learned_start_8x8x8"] = run_learned_eval(sub, T, dev, rank)
+        line["reference_logged_stages"] = run_reference_stages(sub, T, dev, rank)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

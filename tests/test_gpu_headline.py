@@ -10,6 +10,9 @@ on to 1e-8 e (the fixed point itself).
 
   - The plain FP64 GPU form runs the same SCC from q0: iterations within 1,
     charges within 1e-6 e, band energy within 1e-7 Ha/atom of the oracle's.
+  - The FP32 form from q0 with the oracle's mixer: iterations within 1,
+    charges within 1e-6 e and band energy within 1e-7 Ha/atom of the
+    oracle's fixed point.
   - The FP32 form from the learned start (another starting point and mixer)
     lands on the same fixed point: charges within 1e-6 e and band energy
     within 1e-7 Ha/atom of the oracle's fixed point.
@@ -47,6 +50,21 @@ def test_plain_fp64_matches_oracle_scc(gpu, cell):
     assert abs(r["iters"] - int(fx["iters"])) <= 1, (r["iters"], int(fx["iters"]))
     assert np.abs(r["q"] - fx["q"]).max() < 1e-6
     assert abs(r["e_band"] - float(fx["e_band"])) / m.natoms < 1e-7
+
+
+def test_fp32_from_q0_matches_oracle_scc(gpu, cell):
+    """The FP32 form from the oracle's own start and mixer (q0, Anderson
+    16 / 0.2): iteration count within 1 of the oracle's, and the charges and
+    band energy of its stopping point within 1e-6 e and 1e-7 Ha/atom of the
+    oracle's fixed point."""
+    m, fx = cell
+    with gpu.Context(M=int(fx["M"]), kT=float(fx["kT"]), precision=gpu.PREC_FP32, mix_beta=0.2,
+                     mix_history=16, scc_tol=1e-6, scc_max_iter=60) as c:
+        c.set_model(m)
+        r = c.scc_solve()
+    assert abs(r["iters"] - int(fx["iters"])) <= 1, (r["iters"], int(fx["iters"]))
+    assert np.abs(r["q"] - fx["q_tight"]).max() < 1e-6
+    assert abs(r["e_band"] - float(fx["e_band_tight"])) / m.natoms < 1e-7
 
 
 def test_fp32_learned_start_matches_oracle_fixed_point(gpu, cell):
