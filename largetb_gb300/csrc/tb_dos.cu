@@ -4,7 +4,9 @@
 // n_random Gaussian probe vectors r (counter-based splitmix64 + Box-Muller:
 // entry i of vector t is deviate t*n + i of the stream seeded with `seed`)
 // form the columns of one slab; the plain FP64 Chebyshev step advances them
-// and k_probe_dot accumulates mu_k = sum_t r_t^T T_k(X) r_t after every step.
+// and k_probe_dot takes per-block shares of mu_k = sum_t r_t^T T_k(X) r_t
+// after every step (summed in block order at the end: the moments are the
+// same from run to run).
 // The DOS at the Chebyshev nodes x_q = cos(pi (q+1/2)/npts) is
 //   rho(x_q) = [g_0 mu_0 + 2 sum_{k>=1} g_k mu_k cos(k acos x_q)] / (pi sqrt(1 - x_q^2))
 // with the closed-form Jackson g_k (N = n_moments), at energies a x_q + b.
@@ -51,10 +53,12 @@ __global__ void k_probe_init(double *__restrict__ T0, double *__restrict__ R, in
     }
 }
 
-// mom_k += sum_{i,t} R[i][t] T_k[i][t]
+// part_k[block] = this block's share of sum_{i,t} R[i][t] T_k[i][t]; the
+// shares are summed in block order by k_sum_parts, so the moments do not
+// depend on the order in which blocks finish.
 __global__ void __launch_bounds__(256) k_probe_dot(const double *__restrict__ R,
                                                    const double *__restrict__ Tk, int64_t tot,
-                                                   double *__restrict__ mom_k)
+                                                   double *__restrict__ part_k)
 {
     __shared__ double sh[8];
     double s = 0.0;
@@ -67,7 +71,26 @@ __global__ void __launch_bounds__(256) k_probe_dot(const double *__restrict__ R,
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int w = 0; w < 8; w++) t += sh[w];
-        atomicAdd(mom_k, t);
+        part_k[blockIdx.x] = t;
+    }
+}
+
+// mom[k] = sum over blocks of part[k][block], one CTA per moment, a fixed
+// tree order.
+__global__ void __launch_bounds__(256) k_sum_parts(const double *__restrict__ part, int nparts,
+                                                   double *__restrict__ mom)
+{
+    __shared__ double sh[8];
+    const double *p = part + (int64_t)blockIdx.x * nparts;
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x) s += p[b];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; w++) t += sh[w];
+        mom[blockIdx.x] = t;
     }
 }
 
@@ -208,16 +231,19 @@ int run_density_stochastic(tb_ctx *ctx, const double *d_shift, int nr, uint64_t 
     const int B_dos = ((nr + 63) / 64) * 64;
     const int B = std::min(B_dos, Bmax);
     double *T0 = nullptr, *T1 = nullptr, *R = nullptr, *mom = nullptr, *gd = nullptr, *E = nullptr,
-           *dos = nullptr, *num = nullptr, *den = nullptr;
+           *dos = nullptr, *num = nullptr, *den = nullptr, *part = nullptr;
     int rc = TB_OK;
     cudaError_t e = cudaSuccess;
     int64_t nl = 0;
     const int64_t slab = (int64_t)m.n * std::max(B_dos, B);
+    const int64_t tot = (int64_t)m.n * B_dos;
+    const int blocks = (int)std::min<int64_t>((tot + 255) / 256, 152 * 8);
     if ((e = cudaMalloc(&T0, sizeof(double) * slab)) || (e = cudaMalloc(&T1, sizeof(double) * slab)) ||
         (e = cudaMalloc(&R, sizeof(double) * slab)) || (e = cudaMalloc(&mom, sizeof(double) * nmom_dos)) ||
         (e = cudaMalloc(&gd, sizeof(double) * nmom_dos)) || (e = cudaMalloc(&E, sizeof(double) * npts)) ||
         (e = cudaMalloc(&dos, sizeof(double) * npts)) || (e = cudaMalloc(&num, sizeof(double) * m.n)) ||
-        (e = cudaMalloc(&den, sizeof(double) * m.n))) {
+        (e = cudaMalloc(&den, sizeof(double) * m.n)) ||
+        (e = cudaMalloc(&part, sizeof(double) * (size_t)blocks * nmom_dos))) {
         ctx->err = std::string("cudaMalloc(stochastic density): ") + cudaGetErrorString(e);
         rc = e == cudaErrorMemoryAllocation ? TB_ERR_OUT_OF_MEMORY : TB_ERR_CUDA;
     }
@@ -232,22 +258,21 @@ int run_density_stochastic(tb_ctx *ctx, const double *d_shift, int nr, uint64_t 
         for (int k = 0; k < nmom_dos; k++)
             gh[k] = ((N - k + 1) * std::cos(kPi * k / (N + 1)) + std::sin(kPi * k / (N + 1)) * cotv) / (N + 1);
         cudaMemcpyAsync(gd, gh.data(), sizeof(double) * nmom_dos, cudaMemcpyHostToDevice, st);
-        cudaMemsetAsync(mom, 0, sizeof(double) * nmom_dos, st);
         launch_gershgorin(st, m, d_shift, ctx->p.spectral_pad, ctx->p.kT, M, w.nq_cap, w.state, ctx->p.bounds_lo,
                           ctx->p.bounds_hi);
         launch_build_x(st, m, d_shift, TB_PREC_FP64, w.state);
-        const int64_t tot = (int64_t)m.n * B_dos;
-        const int blocks = (int)std::min<int64_t>((tot + 255) / 256, 152 * 8);
         k_probe_init<<<blocks, 256, 0, st>>>(T0, R, m.n, B_dos, nr, seed);
-        k_probe_dot<<<blocks, 256, 0, st>>>(R, T0, tot, mom);
+        k_probe_dot<<<blocks, 256, 0, st>>>(R, T0, tot, part);
         nl += 4;
         for (int kout = 1; kout < nmom_dos; kout++) {
             const bool odd = kout & 1;
             double *in = odd ? T0 : T1, *out = odd ? T1 : T0;
             launch_cheb_step_f64(st, m, in, out, B_dos, m.n, kout == 1, nullptr, kout);
-            k_probe_dot<<<blocks, 256, 0, st>>>(R, out, tot, mom + kout);
+            k_probe_dot<<<blocks, 256, 0, st>>>(R, out, tot, part + (int64_t)kout * blocks);
             nl += (kout == 1) ? 3 : 2;
         }
+        k_sum_parts<<<nmom_dos, 256, 0, st>>>(part, blocks, mom);
+        nl++;
         k_dos_eval<<<(npts + 127) / 128, 128, 0, st>>>(gd, mom, nmom_dos, npts, w.state, E, dos);
         // ---- mu and the refined interval; X on it; the expansion coefficients ----
         k_dos_mu<<<1, 1, 0, st>>>(E, dos, npts, m.n, ctx->p.n_electrons, ctx->p.kT, M, w.nq_cap, w.state);
@@ -289,6 +314,7 @@ int run_density_stochastic(tb_ctx *ctx, const double *d_shift, int nr, uint64_t 
     cudaFree(dos);
     cudaFree(num);
     cudaFree(den);
+    cudaFree(part);
     if (launches) *launches = nl;
     return rc;
 }
@@ -301,15 +327,17 @@ int run_kpm_dos(tb_ctx *ctx, int nmom, int nr, uint64_t seed, int npts, double *
     const int B = ((nr + 63) / 64) * 64;
     const int64_t tot = (int64_t)m.n * B;
     double *T0 = nullptr, *T1 = nullptr, *R = nullptr, *mom = nullptr, *g = nullptr, *E = nullptr,
-           *dos = nullptr;
+           *dos = nullptr, *part = nullptr;
     DevState *state = nullptr;
     int rc = TB_OK;
     cudaError_t e = cudaSuccess;
     int64_t nl = 0;
+    const int blocks = (int)std::min<int64_t>((tot + 255) / 256, 152 * 8);
     if ((e = cudaMalloc(&T0, sizeof(double) * tot)) || (e = cudaMalloc(&T1, sizeof(double) * tot)) ||
         (e = cudaMalloc(&R, sizeof(double) * tot)) || (e = cudaMalloc(&mom, sizeof(double) * nmom)) ||
         (e = cudaMalloc(&g, sizeof(double) * nmom)) || (e = cudaMalloc(&E, sizeof(double) * npts)) ||
-        (e = cudaMalloc(&dos, sizeof(double) * npts)) || (e = cudaMalloc(&state, sizeof(DevState)))) {
+        (e = cudaMalloc(&dos, sizeof(double) * npts)) || (e = cudaMalloc(&state, sizeof(DevState))) ||
+        (e = cudaMalloc(&part, sizeof(double) * (size_t)blocks * nmom))) {
         ctx->err = std::string("cudaMalloc(kpm dos): ") + cudaGetErrorString(e);
         rc = e == cudaErrorMemoryAllocation ? TB_ERR_OUT_OF_MEMORY : TB_ERR_CUDA;
     }
@@ -324,23 +352,22 @@ int run_kpm_dos(tb_ctx *ctx, int nmom, int nr, uint64_t seed, int npts, double *
         for (int k = 0; k < nmom; k++)
             gh[k] = ((N - k + 1) * std::cos(kPi * k / (N + 1)) + std::sin(kPi * k / (N + 1)) * cotv) / (N + 1);
         cudaMemcpyAsync(g, gh.data(), sizeof(double) * nmom, cudaMemcpyHostToDevice, st);
-        cudaMemsetAsync(mom, 0, sizeof(double) * nmom, st);
         launch_gershgorin(st, m, nullptr, 0.0, 0.0, 2, 1 << 22, state, ctx->p.bounds_lo, ctx->p.bounds_hi);
         launch_build_x(st, m, nullptr, TB_PREC_FP64, state);
-        int blocks = (int)std::min<int64_t>((tot + 255) / 256, 152 * 8);
         k_probe_init<<<blocks, 256, 0, st>>>(T0, R, m.n, B, nr, seed);
-        k_probe_dot<<<blocks, 256, 0, st>>>(R, T0, tot, mom);
+        k_probe_dot<<<blocks, 256, 0, st>>>(R, T0, tot, part);
         nl += 4;
         for (int kout = 1; kout < nmom; kout++) {
             const bool odd = kout & 1;
             double *in = odd ? T0 : T1, *out = odd ? T1 : T0;
             // c0 = n: no identity diagonal to gather for probe vectors
             launch_cheb_step_f64(st, m, in, out, B, m.n, kout == 1, nullptr, kout);
-            k_probe_dot<<<blocks, 256, 0, st>>>(R, out, tot, mom + kout);
+            k_probe_dot<<<blocks, 256, 0, st>>>(R, out, tot, part + (int64_t)kout * blocks);
             nl += (kout == 1) ? 3 : 2;
         }
+        k_sum_parts<<<nmom, 256, 0, st>>>(part, blocks, mom);
         k_dos_eval<<<(npts + 127) / 128, 128, 0, st>>>(g, mom, nmom, npts, state, E, dos);
-        nl++;
+        nl += 2;
         DevState hs;
         cudaMemcpyAsync(mom_h, mom, sizeof(double) * nmom, cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(E_h, E, sizeof(double) * npts, cudaMemcpyDeviceToHost, st);
@@ -366,6 +393,7 @@ int run_kpm_dos(tb_ctx *ctx, int nmom, int nr, uint64_t seed, int npts, double *
     cudaFree(E);
     cudaFree(dos);
     cudaFree(state);
+    cudaFree(part);
     if (launches) *launches = nl;
     return rc;
 }

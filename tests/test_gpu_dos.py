@@ -24,6 +24,22 @@ def test_kpm_dos_matches_oracle(gpu):
     np.testing.assert_allclose(r["dos"], dos, atol=1e-8 * np.abs(dos).max(), rtol=0)
 
 
+def test_stochastic_paths_repeat_bitwise(gpu):
+    """The same probes give the same moments, DOS, mu and charges from run
+    to run: the per-step probe dots are summed in a fixed order."""
+    m = gpu.model_cristobalite(2, 2, 2, sigma_ang=0.05, seed=1001)
+    with gpu.Context(M=120, kT=0.01, precision=gpu.PREC_FP64) as c:
+        c.set_model(m)
+        d1 = c.kpm_dos(n_moments=300, n_random=64, seed=5, npts=600)
+        d2 = c.kpm_dos(n_moments=300, n_random=64, seed=5, npts=600)
+        s1 = c.density_stochastic(n_probes=64, seed=9, dos_moments=300, dos_points=600)
+        s2 = c.density_stochastic(n_probes=64, seed=9, dos_moments=300, dos_points=600)
+    np.testing.assert_array_equal(d1["moments"], d2["moments"])
+    np.testing.assert_array_equal(d1["dos"], d2["dos"])
+    assert s1["mu"] == s2["mu"]
+    np.testing.assert_array_equal(s1["q"], s2["q"])
+
+
 def test_kpm_dos_statistics(gpu):
     """The stochastic trace estimates tr T_k(X): mu_0 / n_random ~ n and the
     integrated DOS ~ n (up to sampling noise)."""
