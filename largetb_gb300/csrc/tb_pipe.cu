@@ -443,6 +443,14 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
     // ---------------- consumers ----------------
     const int c = 2 * lane;
     bool gave_up = false;  // this warp has passed over a tile that was never issued
+    // batched form: the next tile's descriptor and group header, loaded one
+    // tile ahead so that their latency overlaps the current tile
+    PipeBatchTile bt_next{};
+    int4 hb_next = make_int4(0, 0, 0, 0);
+    if (kBatch && total > 0) {
+        bt_next = a.tiles[tile_of_task<kMulti>(a, ntiles, 0, mine)];
+        hb_next = __ldg(a.hdr + 2 * bt_next.g + 1);
+    }
     for (int i = 0; i < total; ++i) {
         const int k = a.k0 + i / mine;
         const int t = tile_of_task<kMulti>(a, ntiles, i, mine);
@@ -450,8 +458,12 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         int g, I0, nr;
         int64_t coff, pbase;  // slab offset of the tile's chunk; float2 offset of its column sums
         if constexpr (kBatch) {
-            const PipeBatchTile bt = a.tiles[t];
-            const int4 hb = __ldg(a.hdr + 2 * bt.g + 1);
+            const PipeBatchTile bt = bt_next;
+            const int4 hb = hb_next;
+            if (i + 1 < total) {
+                bt_next = a.tiles[tile_of_task<kMulti>(a, ntiles, i + 1, mine)];
+                hb_next = __ldg(a.hdr + 2 * bt_next.g + 1);
+            }
             g = bt.g;
             coff = bt.coff;
             pbase = bt.pbase;
