@@ -464,10 +464,11 @@ __global__ void __launch_bounds__(1024) k_sp2_scan(int n, const int32_t *__restr
 }
 
 // The numeric step: one CTA per output block row I (grid-stride, heavy rows
-// first), one warp per output block (I, J), J >= I.  The warp walks row I's
-// columns K 32 at a time, tests each against row J's bitmap, and appends the
-// hits (positions of K in rows I and J) to a 64-entry list through a ballot;
-// every 32 entries each lane forms one block product.  Writes the new block
+// first), one warp per output block (I, J), J >= I.  The warp ANDs the
+// bitmap words of rows I and J, 32 words at a time (one per lane), and each
+// lane expands its word's common bits into list entries (positions of K in
+// rows I and J, from the prefix counts) at its scanned offset; every 32
+// entries each lane forms one block product.  Writes the new block
 // (X^2 or 2X - X^2) at (I, J) and its transpose at (J, I) of the uncompacted
 // output (row pointers optr over the pattern OB), the keep flag of both, and
 // counts kept blocks per row.
@@ -486,23 +487,19 @@ __global__ void __launch_bounds__(32 * kNumWarps)
     extern __shared__ __align__(16) unsigned char smraw[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     T *sA = reinterpret_cast<T *>(smraw);                                   // a_cap x 16 (planes)
-    int32_t *sK = reinterpret_cast<int32_t *>(sA + (size_t)a_cap * 16);    // a_cap columns of row I
-    uint32_t *sRB = reinterpret_cast<uint32_t *>(sK + a_cap);              // nw
+    uint32_t *sRB = reinterpret_cast<uint32_t *>(sA + (size_t)a_cap * 16); // nw
     int32_t *sRP = reinterpret_cast<int32_t *>(sRB + nw);                  // nw
     uint32_t *sOB = reinterpret_cast<uint32_t *>(sRP + nw);                // nw
     int32_t *sOP = reinterpret_cast<int32_t *>(sOB + nw);                  // nw
     // per warp: row J's blocks of two product rounds (2 x 32 entries x 8
     // pairs, [pair][entry]), the intersection list (l_cap), its J items
-    // (kJCap), row J's bitmap and prefix counts
-    const size_t wbase = ((size_t)a_cap * (16 * sizeof(T) + 4) + 16 * (size_t)nw + 15) & ~(size_t)15;
-    const size_t wstride = (512 * sizeof(P2) + 4 * ((size_t)l_cap + kJCap + 2 * nw) + 15) & ~(size_t)15;
+    // (kJCap)
+    const size_t wbase = ((size_t)a_cap * 16 * sizeof(T) + 16 * (size_t)nw + 15) & ~(size_t)15;
+    const size_t wstride = (512 * sizeof(P2) + 4 * ((size_t)l_cap + kJCap) + 15) & ~(size_t)15;
     P2 *wB = reinterpret_cast<P2 *>(smraw + wbase + (size_t)w * wstride);
     uint32_t *list = reinterpret_cast<uint32_t *>(wB + 512);
     int32_t *jl = reinterpret_cast<int32_t *>(list + l_cap);               // kJCap
-    uint32_t *wRB = reinterpret_cast<uint32_t *>(jl + kJCap);              // nw
-    int32_t *wRP = reinterpret_cast<int32_t *>(wRB + nw);                  // nw
     const int e = (lane >> 1) & 15, er = e >> 2, ec = e & 3;  // the element this lane ends with
-    const uint32_t lt_mask = (1u << lane) - 1u;
     const float drop2f = (float)drop2;
     double trX2 = 0.0, idem2 = 0.0, trNew = 0.0;
     float ih = 0.f, il = 0.f;
@@ -516,7 +513,6 @@ __global__ void __launch_bounds__(32 * kNumWarps)
             int4 *dst = reinterpret_cast<int4 *>(sA);
             const int n16 = li * (int)sizeof(T);  // li blocks x 16 elements / 16 bytes
             for (int i = threadIdx.x; i < n16; i += blockDim.x) dst[i] = __ldg(src + i);
-            for (int i = threadIdx.x; i < li; i += blockDim.x) sK[i] = xcol[ri + i];
         }
         for (int i = threadIdx.x; i < nw; i += blockDim.x) {
             sRB[i] = RB[(size_t)I * nw + i];
@@ -527,7 +523,6 @@ __global__ void __launch_bounds__(32 * kNumWarps)
         __syncthreads();
         const P2 *Ab = reinterpret_cast<const P2 *>(staged ? sA : xblk + (size_t)ri * 16);
         const T *At = reinterpret_cast<const T *>(Ab);
-        const int32_t *Kl = staged ? sK : xcol + ri;
         const int obase = optr[I];
         // the output columns J >= I of row I, item k to warp k % kNumWarps
         int item0 = 0;
@@ -556,35 +551,38 @@ __global__ void __launch_bounds__(32 * kNumWarps)
                 const int J = jl[jj];
                 const int rj = xptr[J], lj = xptr[J + 1] - rj;
                 const P2 *Bb = reinterpret_cast<const P2 *>(xblk + (size_t)rj * 16);
-                // row J's bitmap and prefix counts into this warp's shared memory
-                for (int i = lane; i < nw; i += 32) {
-                    wRB[i] = __ldg(RB + (size_t)J * nw + i);
-                    wRP[i] = __ldg(RP + (size_t)J * nw + i);
-                }
-                __syncwarp();
+                const uint32_t *RBJ = RB + (size_t)J * nw;
+                const int32_t *RPJ = RP + (size_t)J * nw;
                 Acc acc[16];
                 acc_zero(acc);
                 unsigned long long nprod = 0;
-                for (int seg = 0; seg < li; seg += l_cap) {
-                    // row I's columns K in [seg, seg + l_cap) that row J also holds
+                // segments of whole bitmap words whose intersection fits the list:
+                // all of them when row I is staged (the intersection is at most
+                // li <= l_cap entries), else l_cap / 32 words (<= l_cap entries)
+                const int W = staged ? nw : max(1, l_cap >> 5);
+                for (int w0 = 0; w0 < nw; w0 += W) {
+                    // the K held by both rows: AND of their bitmap words; each
+                    // lane expands its word's bits into (position in row I,
+                    // position in row J) entries at its prefix offset, so the
+                    // list runs in increasing K as row I's columns do
                     int cnt_l = 0;
-                    const int segend = min(li, seg + l_cap);
-                    // two rounds of 32 candidates per iteration: independent chains
-                    for (int t0 = seg; t0 < segend; t0 += 64) {
-                        const int pa = t0 + lane, pb = t0 + 32 + lane;
-                        const int Ka = pa < segend ? Kl[pa] : -1;
-                        const int Kb = pb < segend ? Kl[pb] : -1;
-                        const uint32_t wa = Ka >= 0 ? wRB[Ka >> 5] : 0u, ba = 1u << (Ka & 31);
-                        const uint32_t wb = Kb >= 0 ? wRB[Kb >> 5] : 0u, bb = 1u << (Kb & 31);
-                        const bool ha = wa & ba, hb = wb & bb;
-                        const uint32_t ea = ha ? ((uint32_t)pa << 16) | (uint32_t)(wRP[Ka >> 5] + __popc(wa & (ba - 1u))) : 0u;
-                        const uint32_t eb = hb ? ((uint32_t)pb << 16) | (uint32_t)(wRP[Kb >> 5] + __popc(wb & (bb - 1u))) : 0u;
-                        const uint32_t bal_a = __ballot_sync(0xffffffffu, ha);
-                        const uint32_t bal_b = __ballot_sync(0xffffffffu, hb);
-                        const int na = __popc(bal_a);
-                        if (ha) list[cnt_l + __popc(bal_a & lt_mask)] = ea;
-                        if (hb) list[cnt_l + na + __popc(bal_b & lt_mask)] = eb;
-                        cnt_l += na + __popc(bal_b);
+                    const int wend = min(nw, w0 + W);
+                    for (int c0 = w0; c0 < wend; c0 += 32) {
+                        const int wi = c0 + lane;
+                        const uint32_t bI = wi < wend ? sRB[wi] : 0u;
+                        const uint32_t bJ = wi < wend ? __ldg(RBJ + wi) : 0u;
+                        uint32_t both = bI & bJ;
+                        const int pI = both ? sRP[wi] : 0, pJ = both ? __ldg(RPJ + wi) : 0;
+                        const int c = __popc(both);
+                        const int incl = warp_incl_scan(c, lane);
+                        int o = cnt_l + incl - c;
+                        while (both) {
+                            const uint32_t below = (both & (0u - both)) - 1u;  // bits under the lowest set bit
+                            both &= both - 1u;
+                            list[o++] = ((uint32_t)(pI + __popc(bI & below)) << 16) |
+                                        (uint32_t)(pJ + __popc(bJ & below));
+                        }
+                        cnt_l += __shfl_sync(0xffffffffu, incl, 31);
                     }
                     __syncwarp();
                     // the block products: 32 entries per round, each lane's B block
@@ -802,8 +800,8 @@ cudaError_t csr_reserve(Sp2Csr &b, int nb, long long cap, size_t es)
 size_t numeric_smem(int a_cap, int l_cap, int nw, size_t es)
 {
     // the kernel's own layout: staged row, four bitmaps, then per-warp areas
-    const size_t base = ((size_t)a_cap * (16 * es + 4) + 16 * (size_t)nw + 15) & ~(size_t)15;
-    const size_t stride = (512 * 2 * es + 4 * ((size_t)l_cap + kJCap + 2 * nw) + 15) & ~(size_t)15;
+    const size_t base = ((size_t)a_cap * 16 * es + 16 * (size_t)nw + 15) & ~(size_t)15;
+    const size_t stride = (512 * 2 * es + 4 * ((size_t)l_cap + kJCap) + 15) & ~(size_t)15;
     return base + (size_t)kNumWarps * stride;
 }
 
@@ -939,7 +937,7 @@ int sp2_run(tb_ctx *ctx, double *diagP_h, double *q_h, double *e_band, tb_report
         {
             // stage row I in shared memory and keep whole intersection lists
             // (l_cap = a_cap entries) when both fit: two CTAs per SM if possible
-            const size_t per_blk = 16 * sizeof(T) + 4 + 4 * kNumWarps;
+            const size_t per_blk = 16 * sizeof(T) + 4 * kNumWarps;
             const size_t fixed = numeric_smem(0, 0, nw, sizeof(T));
             const size_t half = (size_t)dev_smem / 2 > fixed + 1024 ? (size_t)dev_smem / 2 - fixed - 1024 : 0;
             int a_cap = (int)std::min<size_t>((size_t)hs.maxlen, ((size_t)dev_smem - fixed - 1024) / per_blk);
