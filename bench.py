@@ -85,6 +85,32 @@ def peaks():
         return 6800.0, "fallback"
 
 
+_FP64_PEAK = {}
+
+
+def fp64_peak(device):
+    """FP64 FMA rate of the CUDA cores (TFLOP/s), measured by libtb_peaks.so
+    (eight register-resident FMA chains per thread, best of three launches):
+    the roofline of the FP64 paths.  None if the helper is missing."""
+    if device not in _FP64_PEAK:
+        import ctypes
+        path = os.path.join(ROOT, "largetb_gb300", "_build", "libtb_peaks.so")
+        val = None
+        if os.path.exists(path):
+            out = ctypes.c_double(0.0)
+            if ctypes.CDLL(path).tb_peak_fp64_fma(int(device), ctypes.byref(out)) == 0:
+                val = out.value
+        _FP64_PEAK[device] = val
+    return _FP64_PEAK[device]
+
+
+def fp64_roofline(flop, seconds, device):
+    rate = flop / seconds / 1e12
+    pk = fp64_peak(device)
+    return {"fp64_tflops": rate, "fp64_fma_peak_tflops": pk, "frac_fp64_peak": rate / pk if pk else None,
+            "flop": flop}
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region (read-only queries)."""
 
@@ -332,12 +358,15 @@ def run_reference_stages(args, T, dev, rank):
     c.close()
     t_all = r["report"]["t_total_ms"] / 1e3
     ref = REFERENCE_LOGGED
+    nnzb = int(m.rowptr[-1]) // 16
+    cols = (500 + 63) // 64 * 64  # the probes in whole 64-column slabs
     return {"metric": "s per stage, the reference's logged workload (8x8x8 alpha-quartz, 500 vectors)",
             "config": {"cells": [8, 8, 8], "atoms": m.natoms, "orbitals": m.n, "vectors": 500,
                        "dos_moments": 1000, "M": 200, "kT": 0.0, "precision": "fp64"},
             "kpm_dos_s": t_kpm, "density_s": t_all - t_kpm, "dos_plus_density_s": t_all,
             "electrons": float(r["q"].sum()), "n_electrons": m.n_electrons,
             "reference_logged": ref,
+            "kpm_dos_roofline": fp64_roofline(999.0 * nnzb * 32.0 * cols, t_kpm, dev),
             "ratio_kpm_dos": ref["kpm_dos_s"] / t_kpm,
             "ratio_density": ref["first_density_s"] / max(t_all - t_kpm, 1e-9)}
 
@@ -674,6 +703,10 @@ def main():
                               "speedup_fast_vs_plain": rep64["t_total_ms"] / 1e3 / value,
                               "max_dq_fast_vs_plain": float(np.abs(q32 - r64["q"]).max()),
                               "e_band_diff_per_atom": abs(eb32 - r64["e_band"]) / m.natoms}
+        # the plain form runs M steps per identity column: 32 flop per 4x4 block and column
+        nnzb = int(m.rowptr[-1]) // 16
+        line["plain_fp64"]["roofline"] = fp64_roofline(
+            float(r64["iters"]) * M * nnzb * 32.0 * m.n, rep64["t_moments_ms"] / 1e3, dev)
         # FP32 error alone: both forms on the same H (H0 + Gamma shift of the FP32 charges)
         shift = ctx.coulomb_shift(q32)[m.orb2atom]
         d32, d64 = ctx.density(shift), ctx64.density(shift)

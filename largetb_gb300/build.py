@@ -17,6 +17,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libtb_gb300.so")
+# measurement helper beside the library (not part of include/largetb.h)
+PEAKS_SRC = "tb_peaks.cu"
+PEAKS_LIB = os.path.join(OUT_DIR, "libtb_peaks.so")
 SOURCES = ["tb_api.cpp", "tb_model.cpp", "tb_kpe.cu", "tb_sp2.cu", "tb_dos.cu", "tb_batch.cu", "tb_geom.cu", "tb_mlp.cu", "tb_noalloc.cu", "tb_pipe.cu", "tb_mlp_tc.cu"]
 HEADERS = ["tb_internal.h", "tb_abi_guard.h", "tb_f32x2.cuh", os.path.join("..", "..", "include", "largetb.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -67,6 +70,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(" ".join(cmd))
             print(res.stdout + res.stderr)
             raise RuntimeError("link of libtb_gb300.so failed")
+    psrc = os.path.join(CSRC, PEAKS_SRC)
+    if os.path.exists(psrc) and (force or _stale(PEAKS_LIB, [psrc])):
+        cmd = [nvcc(), *_flags(), "-shared", "-cudart", "static", "-o", PEAKS_LIB, psrc]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            print(" ".join(cmd))
+            print(res.stdout + res.stderr)
+            raise RuntimeError("build of libtb_peaks.so failed")
     return LIB
 
 
