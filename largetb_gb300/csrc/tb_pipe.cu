@@ -292,7 +292,10 @@ template <bool kBatch, bool kMulti>
 __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    float *red = reinterpret_cast<float *>(smem + (size_t)a.stages * a.stage_bytes);  // [CW][64][2][2]
+    // [CW][2][32][4]: consumer warp w, lane l, column 2l + h at ((2w + h) 32 + l) 4,
+    // holding (<T_k,T_k> hi, lo, <T_k,T_{k+1}> hi, lo); each 16-byte store of a
+    // warp covers 512 contiguous bytes (no bank conflict)
+    float *red = reinterpret_cast<float *>(smem + (size_t)a.stages * a.stage_bytes);
     uint64_t *full = reinterpret_cast<uint64_t *>(red + kPipeCW * kPipeCols * 4);
     uint64_t *empty = full + a.stages;
     uint64_t *pub = empty + a.stages;       // consumers -> publisher: tile done
@@ -524,9 +527,9 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
         // this tile's redfree, and the next phase of redfree needs this warp's
         // arrival on redfull.
         if (i == 0 || wait_phase(redfree, (uint32_t)(i - 1) & 1u, s_abort, a.err)) {
-            float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)warp * kPipeCols + c) * 4);
-            rb[0] = make_float4(eh.x, el.x, oh.x, ol.x);
-            rb[1] = make_float4(eh.y, el.y, oh.y, ol.y);
+            float4 *rb = reinterpret_cast<float4 *>(red + ((size_t)(2 * warp) * 32 + lane) * 4);
+            rb[0] = make_float4(eh.x, el.x, oh.x, ol.x);   // column c
+            rb[32] = make_float4(eh.y, el.y, oh.y, ol.y);  // column c + 1
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(redfull);  // after this warp's T_{k+1} stores of the tile
@@ -535,11 +538,14 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_cheb_f32_pipe(const PipeArg
             // this tile's reducers: (column, which) pairs summed over the
             // consumer warps in warp order
             if (wait_phase(redfull, (uint32_t)i & 1u, s_abort, a.err)) {
-                const int q = rw * 32 + lane, j = q >> 1, which = q & 1;
+                // reducer lane q reads float2 q of every warp's [2][32][4] block:
+                // half h = q / 64, consumer lane l, sum `which` (consecutive lanes,
+                // consecutive addresses); its column is j = 2 l + h
+                const int q = rw * 32 + lane, h = q >> 6, l = (q & 63) >> 1, which = q & 1, j = 2 * l + h;
                 float hsum = 0.f, lsum = 0.f;
 #pragma unroll
                 for (int w = 0; w < kPipeCW; w++) {
-                    const float2 v = *reinterpret_cast<const float2 *>(red + ((size_t)w * kPipeCols + j) * 4 + which * 2);
+                    const float2 v = *reinterpret_cast<const float2 *>(red + (size_t)w * 256 + 2 * q);
                     pair_add(hsum, lsum, v.x);
                     lsum += v.y;
                 }
