@@ -17,6 +17,12 @@ GPU form is solved once beside it.
          event-timed moment passes, against MEASURED_PEAKS.json hbm_gbs
   cpu_baseline  the FP64 CPU oracle (all host threads) on a bounded sample
 
+After the timed region the line also carries the plain FP64 solve (with its
+flop rate against the FP64 FMA rate measured by libtb_peaks.so), the
+distances to the FP64 oracle's fixture, the SP2 purification of 4x4x4, the
+64-cell batch, the 8x8x8 learned-start solve and the reference's logged
+stages on the workload of its log (8x8x8 alpha-quartz, 500 vectors).
+
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
 from __future__ import annotations
