@@ -66,3 +66,17 @@ def test_bad_params_rejected_before_device():
     p = T.params()
     p.struct_size = 8
     assert L.tb_ctx_create(C.byref(p), C.byref(h)) == T.api.TB_ERR_INVALID_ARG
+
+
+def test_peaks_helper_builds_beside_the_library():
+    """libtb_peaks.so (the FP64 FMA-rate probe the benchmark uses) is built by
+    the same build step, exports its one entry and refuses a null output
+    without touching a device."""
+    from largetb_gb300 import build as B
+    B.build()  # incremental: compiles only what is missing or stale
+    path = B.PEAKS_LIB
+    assert os.path.exists(path)
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
+    assert re.search(r"\bT tb_peak_fp64_fma\b", out)
+    L = C.CDLL(path)
+    assert L.tb_peak_fp64_fma(0, None) != 0
