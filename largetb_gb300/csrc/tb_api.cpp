@@ -226,16 +226,26 @@ int autotune(tb_ctx *ctx, int req)
             if ((int)out.size() < 3 && std::find(out.begin(), out.end(), -e.second) == out.end()) out.push_back(-e.second);
         return out;
     };
-    // the FP32 partial array holds K * rowgroups * B pairs of 16 bytes: keep it under 4 GiB
+    // the FP32 partial array holds K * rowgroups * B pairs of 16 bytes: keep it
+    // under a quarter of the free device memory (at least 4 GiB)
     const int Kp = (ctx->p.M + 2) / 2;
-    auto fits = [&](int B, int groups) { return (double)Kp * groups * B * 16.0 <= 4.0 * 1073741824.0; };
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        free_b = 0;
+    }
+    const double part_cap = std::max(4.0 * 1073741824.0, 0.25 * (double)free_b);
+    auto fits = [&](int B, int groups) { return (double)Kp * groups * B * 16.0 <= part_cap; };
     if (prec == TB_PREC_FP32) {
         if ((req == kKindAuto || req == kKindPersistent) && ctx->pp.R > 0) cands.push_back({kKindPersistent, ctx->pp.B});
         if ((req == kKindAuto || req == kKindPipelined) && ctx->pl.stages > 0 && ctx->pl.coop)
             widths(kKindPipelined, {256, 512, 1024}, 64);
         if ((req == kKindAuto || req == kKindPipelinedStep) && ctx->pl.stages > 0) {
             widths(kKindPipelinedStep, {512, 1024}, 64);
-            for (int B : even_widths(768, 4096))
+            // wider slabs amortise each launch's pipeline fill and drain over
+            // more tiles (6x6x6, M = 400: 171.5 ms per density at B = 3456,
+            // 165.6 ms at B = 20736, one slab)
+            for (int B : even_widths(768, n64))
                 if (fits(B, ctx->pl.G)) widths(kKindPipelinedStep, {B}, 64);
         }
         if (req == kKindAuto || req == kKindStaged) widths(kKindStaged, {256, 384, 512}, ctx->sp.R > 0 ? 64 : 128);
@@ -1370,7 +1380,14 @@ int set_hamiltonian_bsr(tb_ctx *ctx, int32_t n, int32_t natoms, const HostBsr &h
     TB_TRY(set_device(ctx));
     free_all(ctx);
     ctx->have_h = ctx->have_scc = false;
-    reset_tuning(ctx);
+    // the autotuner's choice depends on the block pattern only: a new matrix
+    // with the previous pattern (the next geometry of a relaxation, the same
+    // cell again) keeps it
+    if (hb.brow != ctx->tuned_brow || hb.bcol != ctx->tuned_bcol) {
+        reset_tuning(ctx);
+        ctx->tuned_brow = hb.brow;
+        ctx->tuned_bcol = hb.bcol;
+    }
     DevMatrix &m = ctx->m;
     m.n = n;
     m.natoms = natoms;
@@ -1562,6 +1579,8 @@ int tb_set_geometry(tb_ctx *ctx, int32_t natoms, const double *xyz, const int32_
     free_all(ctx);
     ctx->have_h = ctx->have_scc = false;
     reset_tuning(ctx);
+    ctx->tuned_brow.clear();  // a pattern built on the device: no host copy to compare
+    ctx->tuned_bcol.clear();
     GeomDevice g;
     const int rc = geom_build_device(ctx->stream, natoms, xyz, species, box, rcut_bohr, gamma_diag, g, ctx->err);
     DevMatrix &m = ctx->m;

@@ -174,6 +174,7 @@ struct tb_ctx {
     // width (0 = not tuned yet)
     int tuned_kind[2][tb::kNumKinds] = {};
     int tuned_B[2][tb::kNumKinds] = {};
+    std::vector<int32_t> tuned_brow, tuned_bcol;  // block pattern the tuned choices belong to
     // SP2 device scratch (lazily sized)
     // SCC iteration as a CUDA graph: captured once per configuration (gen) and
     // replayed; its moment-phase events are its own, its counts added per replay
