@@ -1521,6 +1521,8 @@ int tb_set_params(tb_ctx *ctx, const tb_params *p)
     ctx->gen++;
     TB_TRY(check_params(ctx, p));
     if (p->device != ctx->device) return fail(ctx, TB_ERR_INVALID_ARG, "device cannot change");
+    // the tuned slab width was admitted for this M's column-sum array (K x G x B)
+    if (p->M != ctx->p.M) reset_tuning(ctx);
     const double ne = ctx->p.n_electrons;
     ctx->p = *p;
     if (!(p->n_electrons > 0) && ctx->have_scc) ctx->p.n_electrons = ne;
