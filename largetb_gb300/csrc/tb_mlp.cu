@@ -51,10 +51,27 @@ __global__ void k_features(int natoms, const double *__restrict__ xyz, const int
     if (i >= natoms) return;
     const double box[3] = {bx, by, bz};
     const double rc = 5.0 * kBohrPerAng, rc2 = rc * rc;
+    // FP32 prefilter of the pair distance (minimum image by a multiply with
+    // the inverse box), with a 1 % margin on rc^2 that covers its rounding;
+    // pairs inside it are recomputed in FP64 below, so the features are the
+    // same as with the FP64 test alone
+    const float fbox[3] = {(float)bx, (float)by, (float)bz};
+    const float finv[3] = {bx > 0 ? (float)(1.0 / bx) : 0.f, by > 0 ? (float)(1.0 / by) : 0.f,
+                           bz > 0 ? (float)(1.0 / bz) : 0.f};
+    const float fi[3] = {(float)xyz[3 * i], (float)xyz[3 * i + 1], (float)xyz[3 * i + 2]};
+    const float rc2_loose = (float)(rc2 * 1.01);
     float f[2 * 16];
     for (int k = 0; k < 32; k++) f[k] = 0.f;
     for (int j = 0; j < natoms; j++) {
         if (j == i) continue;
+        float r2f = 0.f;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            float t = (float)xyz[3 * j + q] - fi[q];
+            t -= fbox[q] * rintf(t * finv[q]);
+            r2f = fmaf(t, t, r2f);
+        }
+        if (r2f >= rc2_loose) continue;
         double d[3];
         for (int q = 0; q < 3; q++) {
             double t = xyz[3 * j + q] - xyz[3 * i + q];
