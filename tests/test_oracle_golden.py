@@ -192,3 +192,41 @@ def test_headline_oracle_fixture_is_this_model():
     assert fx["dq_hist"][-1] < float(fx["tight_tol"])
     assert abs(fx["q"].sum() - m.n_elec) < 1e-6
     assert np.abs(fx["q"] - fx["q_tight"]).max() < 1e-6
+
+
+def _dos_mu_restated(dos, n_elec, n):
+    """runKPM's chemical potential and refined interval from a DOS on the
+    Chebyshev nodes x_i = cos(pi (i + 1/2) / npts) (withSP2_deltaH.cpp:
+    1663-1703), restated in numpy: trapezoid area from the bottom node up,
+    the first node where it reaches N_e / 2n of the total; the interval where
+    DOS / n >= 0.001 first holds from either end (-10, 10 if never)."""
+    npts = len(dos)
+    x = np.cos(np.pi * (np.arange(npts) + 0.5) / npts)
+    seg = (x[:-1] - x[1:]) * (dos[1:] + dos[:-1]) / 2  # segment i-1..i, for i = npts-1 .. 1
+    area = n_elec * seg.sum() / (2.0 * n)
+    cum = np.cumsum(seg[::-1])  # from the bottom node upwards
+    hit = np.nonzero(cum >= area)[0]
+    mi = (npts - 1 - hit[0]) if len(hit) else 0
+    above = np.nonzero(dos / n >= 0.001)[0]
+    lo_i = above.max() if len(above) else None
+    hi_i = above.min() if len(above) else None
+    return mi, lo_i, hi_i, x
+
+
+@pytest.mark.parametrize("gap", [0.0, 0.4])
+def test_dos_mu_matches_a_restatement_of_the_area_rule(gap):
+    """The oracle's mu and interval (orc_dos_mu) against an independent
+    numpy restatement of runKPM's rule, on a two-band DOS (valence and
+    conduction Gaussians, with and without a gap) evaluated on the nodes."""
+    npts, n, n_elec = 2000, 768, 1024.0
+    a, b = 1.3, -0.4
+    x = np.cos(np.pi * (np.arange(npts) + 0.5) / npts)
+    E = a * x + b
+    dos = (2 * n / 3) * np.exp(-((x + 0.35 + gap / 2) / 0.12) ** 2) + (n / 3) * np.exp(-((x - 0.35 - gap / 2) / 0.1) ** 2)
+    r = O.dos_mu(E, dos, n_elec, n)
+    mi, lo_i, hi_i, _ = _dos_mu_restated(dos, n_elec, n)
+    assert r["mu_index"] == mi and r["mu"] == E[mi]
+    assert abs(r["a"] - (E[hi_i] - E[lo_i]) / 2) < 1e-12
+    assert abs(r["b"] - (E[hi_i] + E[lo_i]) / 2) < 1e-12
+    # mu sits where the valence band's share of the area is exhausted
+    assert E[mi] < b + a * (0.35 + gap / 2)
