@@ -30,8 +30,9 @@ __global__ void __launch_bounds__(256) k_fp64_fma_chains(int iters, double seed,
 
 }  // namespace
 
-// FP64 FMA rate of `device` in TFLOP/s (2 flop per FMA).  Returns 0, or the
-// CUDA error code.
+// FP64 FMA rate of `device` in TFLOP/s (2 flop per FMA), on the legacy
+// default stream; makes `device` current for the calling thread.  Returns 0,
+// or the CUDA error code.
 extern "C" int tb_peak_fp64_fma(int device, double *tflops)
 {
     if (!tflops) return (int)cudaErrorInvalidValue;
